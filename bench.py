@@ -1,0 +1,336 @@
+"""Benchmark: FGP-TV 3D on a 512^3 float32 volume (voxel-iterations per second).
+
+Workload (one "step" = one full regulariser call): the seeded 30-ellipsoid
+phantom plus N(0, 0.05^2) noise at 512^3, lambda 0.03, isotropic TV,
+nonnegativity on, up to 500 iterations with the stopping rule epsil = 1e-6
+(the reference's stopping rule decides how many iterations run).
+
+  value     voxel-iterations/s with input and output resident in HBM
+            (device-pointer C ABI, cilreg_fgp_tv_dev), CUDA events on the stream
+  e2e       the same metric through the reference-facing C ABI
+            (TV_FGP_GPU_main) from pinned host buffers, copies included
+  roofline  the FGP iteration kernel: 40 algorithmic bytes per voxel-iteration
+            (read P^{k-1}(3), P^{k-2}(3), f; write P^k(3)) over its average
+            launch time, against the measured HBM copy bandwidth
+  cpu_baseline  the reference's C-OMP FGP (oracle/_ref when it is built for
+            this machine, else the oracle's C restatement) on all host cores,
+            a bounded sample of the same workload
+
+Multi-GPU: one process per GPU (torchrun), each an independent replica of the
+workload (the toolkit's multi-GPU model is one volume per GPU, no exchange);
+value = all ranks' voxel-iterations / the slowest rank's time.
+
+``--impl reference`` times the reference CPU implementation on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ccpi-regularisation-toolkit_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "FGP_TV 3D voxel-iterations/s"
+UNIT = "voxel-iter/s"
+LAM, MAX_ITERS, EPSIL, METHOD, NONNEG = 0.03, 500, 1e-6, 0, 1
+BYTES_PER_VOXEL_ITER = 40  # FGP 3D fused iteration: 7 float reads + 3 float writes
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def _phantom(size):
+    from ccpi.supp.phantoms import noisy_phantom
+
+    return noisy_phantom((size, size, size), 30, 1)
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _ncu_traffic_per_voxel():
+    """DRAM bytes per voxel-iteration of the FGP kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "fgp_tv_3d_kernel.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_voxel_iter:\s*([0-9.]+)", text)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (median SM clock, throttle reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(x, iters, use_threads=None):
+    """Reference C-OMP FGP on the host (compiled reference if loadable here, else the port)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    kind = "reference" if O.ref_lib() is not None else "port"
+    t = time.perf_counter()
+    O.fgp_tv(x, LAM, iters, 0.0, METHOD, NONNEG, use_ref=(kind == "reference"))
+    dt = time.perf_counter() - t
+    cores = O.num_threads()
+    return x.size * iters / dt, kind, cores, dt
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    x = _phantom(args.size)
+    iters = args.ref_iters
+    for _ in range(args.warmup):
+        cpu_baseline(x, iters)
+    vals, kind, cores, secs = [], None, None, 0.0
+    for _ in range(args.steps):
+        v, kind, cores, dt = cpu_baseline(x, iters)
+        vals.append(v)
+        secs += dt
+    value = x.size * iters * args.steps / secs
+    sample = f"FGP_TV {args.size}^3, {iters} fixed iterations per step (epsil=0), iso, nonneg"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"FGP_TV 3D {args.size}^3 phantom", "lambda": LAM, "iterations_per_step": iters},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--ref-iters", type=int, default=4, help="iterations per reference-arm step")
+    ap.add_argument("--cpu-iters", type=int, default=6, help="iterations of the cpu_baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import ctypes
+
+    import torch
+
+    rank, world, local = _env_rank()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    from ccpi.filters import utils as U
+
+    lib = U.cilregcuda
+    x = _phantom(args.size)
+    n = x.size
+    nx = ny = nz = args.size
+    stream = torch.cuda.current_stream(dev)
+    d_in = torch.from_numpy(x).to(dev)
+    d_out = torch.zeros_like(d_in)
+    info = np.zeros(2, np.float32)
+    info_p = info.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def step(iters=MAX_ITERS, epsil=EPSIL):
+        d_out.zero_()  # U_prev of iteration 0, as the reference's np.zeros_like output
+        st = lib.cilreg_fgp_tv_dev(d_in.data_ptr(), d_out.data_ptr(), info_p, LAM, iters, epsil, METHOD, NONNEG,
+                                   nx, ny, nz, stream.cuda_stream)
+        U.check_status(st)
+        return int(info[0])
+
+    for _ in range(args.warmup):
+        step()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = U.launch_count()
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    iters_run = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        iters_run += step()
+    ev1.record(stream)
+    barrier()
+    launches = U.launch_count() - launches0
+    clock_info = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    t_local = ms / 1e3
+    t_max = t_local
+    total_vi = n * iters_run
+    if pg is not None:
+        tt = torch.tensor([t_local, float(total_vi)], device=dev, dtype=torch.float64)
+        t_all = tt.clone()
+        pg.all_reduce(t_all[:1], op=pg.ReduceOp.MAX)
+        pg.all_reduce(t_all[1:], op=pg.ReduceOp.SUM)
+        t_max, total_vi = float(t_all[0]), float(t_all[1])
+    value = total_vi / t_max
+
+    # steady-state launch time of the FGP iteration kernel: difference of two
+    # fixed-count runs on the same stream (one kernel launch per iteration)
+    def timed(iters):
+        barrier()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(iters, 0.0)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / 1e3
+
+    i1, i2 = 10, 60
+    timed(i1)
+    t1 = min(timed(i1) for _ in range(2))
+    t2 = min(timed(i2) for _ in range(2))
+    per_launch = (t2 - t1) / (i2 - i1)
+    peak, peak_kind = _peaks()
+    achieved = BYTES_PER_VOXEL_ITER * n / per_launch / 1e9
+    tpv = _ncu_traffic_per_voxel()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tpv * n if tpv is not None else None), "peak_kind": peak_kind,
+                "kernel": "FGP iteration (k_fgp_step)", "launch_ms": per_launch * 1e3,
+                "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_ITER * n}
+
+    # end to end through the reference-facing C ABI with pinned host buffers
+    h_in = torch.from_numpy(x).pin_memory()
+    h_out = torch.zeros_like(h_in).pin_memory()
+    fp = ctypes.POINTER(ctypes.c_float)
+    e2e_steps = max(1, min(args.steps, 3))
+    lib.TV_FGP_GPU_main(ctypes.cast(h_in.data_ptr(), fp), ctypes.cast(h_out.data_ptr(), fp), info_p, LAM, MAX_ITERS,
+                        EPSIL, METHOD, NONNEG, local, nx, ny, nz)
+    barrier()
+    e2e_vi = 0
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h_out.zero_()
+        st = lib.TV_FGP_GPU_main(ctypes.cast(h_in.data_ptr(), fp), ctypes.cast(h_out.data_ptr(), fp), info_p, LAM,
+                                 MAX_ITERS, EPSIL, METHOD, NONNEG, local, nx, ny, nz)
+        U.check_status(st)
+        e2e_vi += n * int(info[0])
+    barrier()
+    e2e_t = time.perf_counter() - t0
+    e2e_val = e2e_vi / e2e_t
+    if pg is not None:
+        tt = torch.tensor([e2e_t, float(e2e_vi)], device=dev, dtype=torch.float64)
+        pg.all_reduce(tt[:1], op=pg.ReduceOp.MAX)
+        pg.all_reduce(tt[1:], op=pg.ReduceOp.SUM)
+        e2e_val = float(tt[1]) / float(tt[0])
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, kind, cores, dt = cpu_baseline(x, args.cpu_iters)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": f"FGP_TV {args.size}^3, {args.cpu_iters} fixed iterations (epsil=0), {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"FGP_TV 3D {args.size}^3 ellipsoid phantom + noise", "lambda": LAM,
+                       "max_iterations": MAX_ITERS, "epsil": EPSIL, "methodTV": "iso", "nonneg": NONNEG,
+                       "iterations_per_step": iters_run / args.steps,
+                       "l2": "inputs larger than L2 (state 5.6 GB per replica, L2 126 MB)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * 4 * n, "d2h_bytes_per_step": 4 * n},
+            "gpu_launches": launches,
+            "clocks": clock_info,
+        }
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

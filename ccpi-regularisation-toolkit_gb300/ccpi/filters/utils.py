@@ -1,0 +1,111 @@
+"""Loads the GB300 regulariser libraries (the reference's
+src/Python/ccpi/filters/utils.py:13-23 loads ``libcilreg`` and
+``libcilregcuda`` from this directory the same way).
+
+Both libraries are required: there is no CPU fallback.  If they are missing,
+build them with ``python build.py`` in the package root.
+"""
+import ctypes
+import os
+import platform
+
+if platform.system() != "Linux":
+    raise ImportError(f"unsupported platform: {platform.system()} (this build targets Linux on GB300)")
+
+_here = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_here, "libcilreg.so")
+GPU_LIB_PATH = os.path.join(_here, "libcilregcuda.so")
+
+for _p in (LIB_PATH, GPU_LIB_PATH):
+    if not os.path.exists(_p):
+        raise ImportError(f"{_p} is not built; run `python build.py` in "
+                          f"{os.path.dirname(os.path.dirname(_here))}")
+
+cilreg = ctypes.CDLL(LIB_PATH)
+cilregcuda = ctypes.CDLL(GPU_LIB_PATH)
+
+_F = ctypes.c_float
+_I = ctypes.c_int
+_P = ctypes.POINTER(ctypes.c_float)
+_V = ctypes.c_void_p
+
+# *_CPU_main argument lists (src/Core/regularisers_CPU/*_core.h)
+_CPU_SIGS = {
+    "TV_ROF_CPU_main": [_P, _P, _P, _P, _I, _I, _F, _F, _I, _I, _I],
+    "TV_FGP_CPU_main": [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I, _I],
+    "PDTV_CPU_main": [_P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I],
+    "SB_TV_CPU_main": [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I],
+    "TGV_main": [_P, _P, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I],
+    "Diffusion_CPU_main": [_P, _P, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I],
+    "Diffus4th_CPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I],
+}
+# *_GPU_main argument lists (src/Core/regularisers_GPU/*.h)
+_GPU_SIGS = {
+    "TV_ROF_GPU_main": [_P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I],
+    "TV_FGP_GPU_main": [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I, _I, _I],
+    "TV_PD_GPU_main": [_P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I, _I],
+    "TV_SB_GPU_main": [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I, _I],
+    "TGV_GPU_main": [_P, _P, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I, _I],
+    "NonlDiff_GPU_main": [_P, _P, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I, _I],
+    "Diffus4th_GPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I, _I],
+}
+# device-pointer API (include/cilreg_gb300.h)
+_DEV_SIGS = {
+    "cilreg_rof_tv_dev": [_V, _V, _P, _V, _F, _I, _F, _F, _I, _I, _I, _V],
+    "cilreg_fgp_tv_dev": [_V, _V, _P, _F, _I, _F, _I, _I, _I, _I, _I, _V],
+    "cilreg_pd_tv_dev": [_V, _V, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I, _V],
+    "cilreg_sb_tv_dev": [_V, _V, _P, _F, _I, _F, _I, _I, _I, _I, _V],
+    "cilreg_tgv_dev": [_V, _V, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I, _V],
+    "cilreg_ndf_dev": [_V, _V, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I, _V],
+    "cilreg_diff4th_dev": [_V, _V, _P, _F, _F, _I, _F, _F, _I, _I, _I, _V],
+}
+
+for _lib in (cilreg, cilregcuda):
+    for _name, _args in _CPU_SIGS.items():
+        getattr(_lib, _name).argtypes = _args
+        getattr(_lib, _name).restype = ctypes.c_float
+    for _name, _args in {**_GPU_SIGS, **_DEV_SIGS}.items():
+        getattr(_lib, _name).argtypes = _args
+        getattr(_lib, _name).restype = ctypes.c_int
+    _lib.cilreg_last_error.restype = ctypes.c_char_p
+    _lib.cilreg_version.restype = ctypes.c_char_p
+    _lib.cilreg_device_count.restype = ctypes.c_int
+    _lib.cilreg_launch_count.restype = ctypes.c_longlong
+
+
+class RegulariserError(RuntimeError):
+    """A regulariser call returned a failure status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+
+
+def check_status(status, lib=None) -> None:
+    """Raise for a negative status (ValueError for invalid arguments)."""
+    status = int(status)
+    if status == 0:
+        return
+    msg = (lib or cilregcuda).cilreg_last_error().decode(errors="replace")
+    if status == -2:
+        raise ValueError(msg)
+    raise RegulariserError(status, msg)
+
+
+def version() -> str:
+    return cilregcuda.cilreg_version().decode()
+
+
+def device_count() -> int:
+    return int(cilregcuda.cilreg_device_count())
+
+
+def launch_count() -> int:
+    """Kernels launched so far by the library (both names share one counter only
+    when loaded as one object; each loaded library counts its own launches)."""
+    return int(cilregcuda.cilreg_launch_count()) + int(cilreg.cilreg_launch_count())
+
+
+def loaded_libraries():
+    """Paths of the two native libraries this module loaded."""
+    return [LIB_PATH, GPU_LIB_PATH]

@@ -1,0 +1,261 @@
+// The C ABI: drop-in entry points with the reference's argument lists.
+//
+//  * *_GPU_main    host pointers in/out, explicit gpu_device, int status
+//                  (src/Core/regularisers_GPU/*.h, headers/*.h)
+//  * *_CPU_main    the C-OMP argument lists (src/Core/regularisers_CPU/*_core.h);
+//                  in this library they execute on the GPU selected by
+//                  CILREG_GPU_DEVICE (default 0) and return 0 or a negative status
+//  * cilreg_*_dev  device pointers and a caller stream (cudaStream_t as void*)
+//
+// Every entry point validates its arguments, returns a status instead of
+// printing and continuing, and is safe to call from several host threads
+// (each thread gets its own stream; scratch is stream-ordered).
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/cilreg_gb300.h"
+#include "drivers.cuh"
+
+using namespace cilreg;
+
+namespace cilreg {
+
+int check_dims(int nx, int ny, int nz) {
+    if (nx < 1 || ny < 1 || nz < 0)
+        return fail(ERR_ARG, __FILE__, __LINE__, "invalid dimensions (%d, %d, %d)", nx, ny, nz);
+    return OK;
+}
+
+}  // namespace cilreg
+
+namespace {
+
+Dims dims_of(int nx, int ny, int nz) { return make_dims(nx, ny, nz < 1 ? 1 : nz); }
+
+int default_device() {
+    const char* e = getenv("CILREG_GPU_DEVICE");
+    return e ? atoi(e) : 0;
+}
+
+// Host-pointer wrapper: upload input (and the output buffer when `upload_out`),
+// run `body(d_in, d_out, stream)`, download the output.
+template <class Body>
+int host_call(const float* in, float* out, int dev, const Dims& d, bool upload_out, Body body) {
+    if (!in || !out) return fail(ERR_ARG, __FILE__, __LINE__, "null Input/Output pointer");
+    CILREG_TRY(use_device(dev));
+    cudaStream_t s = thread_stream(dev);
+    int rc;
+    {
+        Scratch io(s);
+        float* d_in = io.floats(d.n);
+        float* d_out = io.floats(d.n);
+        if (!d_in || !d_out) return io.status();
+        const size_t bytes = sizeof(float) * (size_t)d.n;
+        CILREG_CUDA(cudaMemcpyAsync(d_in, in, bytes, cudaMemcpyHostToDevice, s));
+        if (upload_out) CILREG_CUDA(cudaMemcpyAsync(d_out, out, bytes, cudaMemcpyHostToDevice, s));
+        rc = body(d_in, d_out, s);
+        if (rc == 0) {
+            CILREG_CUDA(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, s));
+            CILREG_CUDA(cudaStreamSynchronize(s));
+        }
+    }
+    return rc;
+}
+
+int dev_prologue(const float* in, const float* out, int nx, int ny, int nz) {
+    CILREG_TRY(check_dims(nx, ny, nz));
+    if (!in || !out) return fail(ERR_ARG, __FILE__, __LINE__, "null device pointer");
+    if (in == out) return fail(ERR_ARG, __FILE__, __LINE__, "input and output must be distinct buffers");
+    return OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// library information
+const char* cilreg_last_error(void) { return last_error(); }
+const char* cilreg_version(void) { return "cilreg-gb300 1.0 (sm_103a)"; }
+long long cilreg_launch_count(void) { return launch_count(); }
+int cilreg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// device-pointer API
+int cilreg_rof_tv_dev(const float* d_in, float* d_out, float* infovector, const float* d_lambda, float lambdaPar,
+                      int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return rof_run(d_in, d_out, d_lambda, lambdaPar, iters, tau, epsil, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
+int cilreg_fgp_tv_dev(const float* d_in, float* d_out, float* infovector, float lambdaPar, int iters, float epsil,
+                      int methodTV, int nonneg, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return fgp_run(d_in, d_out, lambdaPar, iters, epsil, methodTV, nonneg, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
+int cilreg_pd_tv_dev(const float* d_in, float* d_out, float* infovector, float lambdaPar, int iters, float epsil,
+                     float lipschitz_const, int methodTV, int nonneg, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return pd_run(d_in, d_out, lambdaPar, iters, epsil, lipschitz_const, methodTV, nonneg, dims_of(dimX, dimY, dimZ),
+                  (cudaStream_t)stream, infovector);
+}
+
+int cilreg_sb_tv_dev(const float* d_in, float* d_out, float* infovector, float mu, int iters, float epsil,
+                     int methodTV, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return sb_run(d_in, d_out, mu, iters, epsil, methodTV, dims_of(dimX, dimY, dimZ), (cudaStream_t)stream,
+                  infovector);
+}
+
+int cilreg_tgv_dev(const float* d_in, float* d_out, float* infovector, float lambdaPar, float alpha1, float alpha0,
+                   int iters, float L2, float epsil, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return tgv_run(d_in, d_out, lambdaPar, alpha1, alpha0, iters, L2, epsil, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
+int cilreg_ndf_dev(const float* d_in, float* d_out, float* infovector, float lambdaPar, float sigmaPar, int iters,
+                   float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return ndf_run(d_in, d_out, lambdaPar, sigmaPar, iters, tau, penaltytype, epsil, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
+int cilreg_diff4th_dev(const float* d_in, float* d_out, float* infovector, float lambdaPar, float sigmaPar,
+                       int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return diff4th_run(d_in, d_out, lambdaPar, sigmaPar, iters, tau, epsil, dims_of(dimX, dimY, dimZ),
+                       (cudaStream_t)stream, infovector);
+}
+
+// ---------------------------------------------------------------------------
+// *_GPU_main: the reference GPU ABI (host pointers)
+int TV_ROF_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iter, float tau, float epsil,
+                    int gpu_device, int N, int M, int Z) {
+    CILREG_TRY(check_dims(N, M, Z));
+    const Dims d = dims_of(N, M, Z);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return rof_run(di, dout, nullptr, lambdaPar, iter, tau, epsil, d, s, infovector);
+    });
+}
+
+int TV_FGP_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iter, float epsil,
+                    int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ) {
+    CILREG_TRY(check_dims(dimX, dimY, dimZ));
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    // FGP never copies Input into Output: with a stopping rule the caller's
+    // Output is U_prev of iteration 0 (FGP_TV_core.c:66,123)
+    return host_call(Input, Output, gpu_device, d, epsil != 0.0f || iter <= 0,
+                     [&](const float* di, float* dout, cudaStream_t s) {
+                         return fgp_run(di, dout, lambdaPar, iter, epsil, methodTV, nonneg, d, s, infovector);
+                     });
+}
+
+int TV_PD_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iter, float epsil,
+                   float lipschitz_const, int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ) {
+    CILREG_TRY(check_dims(dimX, dimY, dimZ));
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return pd_run(di, dout, lambdaPar, iter, epsil, lipschitz_const, methodTV, nonneg, d, s, infovector);
+    });
+}
+
+int TV_SB_GPU_main(float* Input, float* Output, float* infovector, float mu, int iter, float epsil, int methodTV,
+                   int gpu_device, int dimX, int dimY, int dimZ) {
+    CILREG_TRY(check_dims(dimX, dimY, dimZ));
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return sb_run(di, dout, mu, iter, epsil, methodTV, d, s, infovector);
+    });
+}
+
+int TGV_GPU_main(float* U0, float* U, float* infovector, float lambda, float alpha1, float alpha0, int iterationsNumb,
+                 float L2, float epsil, int gpu_device, int dimX, int dimY, int dimZ) {
+    CILREG_TRY(check_dims(dimX, dimY, dimZ));
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    return host_call(U0, U, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return tgv_run(di, dout, lambda, alpha1, alpha0, iterationsNumb, L2, epsil, d, s, infovector);
+    });
+}
+
+int NonlDiff_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, float sigmaPar,
+                      int iterationsNumb, float tau, int penaltytype, float epsil, int gpu_device, int N, int M,
+                      int Z) {
+    CILREG_TRY(check_dims(N, M, Z));
+    const Dims d = dims_of(N, M, Z);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return ndf_run(di, dout, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype, epsil, d, s, infovector);
+    });
+}
+
+int Diffus4th_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, float sigmaPar,
+                       int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z) {
+    CILREG_TRY(check_dims(N, M, Z));
+    const Dims d = dims_of(N, M, Z);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return diff4th_run(di, dout, lambdaPar, sigmaPar, iterationsNumb, tau, epsil, d, s, infovector);
+    });
+}
+
+// ---------------------------------------------------------------------------
+// *_CPU_main: the reference C-OMP ABI, executed on the GPU
+float TV_ROF_CPU_main(float* Input, float* Output, float* infovector, float* lambdaPar, int lambda_is_arr,
+                      int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ) {
+    if (check_dims(dimX, dimY, dimZ) != 0) return (float)ERR_ARG;
+    if (!lambdaPar) return (float)fail(ERR_ARG, __FILE__, __LINE__, "null lambdaPar");
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    const int dev = default_device();
+    return (float)host_call(Input, Output, dev, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        if (!lambda_is_arr) return rof_run(di, dout, nullptr, *lambdaPar, iterationsNumb, tau, epsil, d, s, infovector);
+        Scratch sc(s);
+        float* dl = sc.floats(d.n);
+        if (!dl) return sc.status();
+        CILREG_CUDA(cudaMemcpyAsync(dl, lambdaPar, sizeof(float) * d.n, cudaMemcpyHostToDevice, s));
+        return rof_run(di, dout, dl, 0.0f, iterationsNumb, tau, epsil, d, s, infovector);
+    });
+}
+
+float TV_FGP_CPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iterationsNumb, float epsil,
+                      int methodTV, int nonneg, int dimX, int dimY, int dimZ) {
+    return (float)TV_FGP_GPU_main(Input, Output, infovector, lambdaPar, iterationsNumb, epsil, methodTV, nonneg,
+                                  default_device(), dimX, dimY, dimZ);
+}
+
+float PDTV_CPU_main(float* Input, float* U, float* infovector, float lambdaPar, int iterationsNumb, float epsil,
+                    float lipschitz_const, int methodTV, int nonneg, int dimX, int dimY, int dimZ) {
+    return (float)TV_PD_GPU_main(Input, U, infovector, lambdaPar, iterationsNumb, epsil, lipschitz_const, methodTV,
+                                 nonneg, default_device(), dimX, dimY, dimZ);
+}
+
+float SB_TV_CPU_main(float* Input, float* Output, float* infovector, float mu, int iter, float epsil, int methodTV,
+                     int dimX, int dimY, int dimZ) {
+    return (float)TV_SB_GPU_main(Input, Output, infovector, mu, iter, epsil, methodTV, default_device(), dimX, dimY,
+                                 dimZ);
+}
+
+float TGV_main(float* U0, float* U, float* infovector, float lambda, float alpha1, float alpha0, int iter, float L2,
+               float epsil, int dimX, int dimY, int dimZ) {
+    return (float)TGV_GPU_main(U0, U, infovector, lambda, alpha1, alpha0, iter, L2, epsil, default_device(), dimX,
+                               dimY, dimZ);
+}
+
+float Diffusion_CPU_main(float* Input, float* Output, float* infovector, float lambdaPar, float sigmaPar,
+                         int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ) {
+    return (float)NonlDiff_GPU_main(Input, Output, infovector, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype,
+                                    epsil, default_device(), dimX, dimY, dimZ);
+}
+
+float Diffus4th_CPU_main(float* Input, float* Output, float* infovector, float lambdaPar, float sigmaPar,
+                         int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ) {
+    return (float)Diffus4th_GPU_main(Input, Output, infovector, lambdaPar, sigmaPar, iterationsNumb, tau, epsil,
+                                     default_device(), dimX, dimY, dimZ);
+}
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+// Device-pointer drivers, one per regulariser.  Every driver:
+//   * takes device pointers and the stream all of its work is enqueued on;
+//   * allocates its state from the stream-ordered pool and frees it on return;
+//   * runs the whole iteration loop without a per-iteration host sync (the
+//     stopping rule is evaluated on the device, see common.cuh);
+//   * writes infovector = [iterations run, last relative change] to the host
+//     pointer `info` (may be null) and returns 0 or a negative Status.
+// The argument meanings are those of the reference's *_CPU_main functions
+// (src/Core/regularisers_CPU/*_core.h), with dims as a Dims value.
+#pragma once
+
+#include "runtime.cuh"
+
+namespace cilreg {
+
+// ROF_TV_core.c:50-99.  lam_arr (device, per voxel) overrides lam when non-null.
+int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
+            const Dims& d, cudaStream_t s, float* info);
+
+// FGP_TV_core.c:40-171.  u_out's initial content is U_prev of iteration 0.
+int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
+            const Dims& d, cudaStream_t s, float* info);
+
+// PD_TV_core.c:40-153
+int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, float lipschitz, int methodTV,
+           int nonneg, const Dims& d, cudaStream_t s, float* info);
+
+// SB_TV_core.c:38-144
+int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int methodTV, const Dims& d,
+           cudaStream_t s, float* info);
+
+// TGV_core.c:43-194
+int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2, float epsil,
+            const Dims& d, cudaStream_t s, float* info);
+
+// Diffusion_core.c:53-102, Jacobi update order
+int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, int penalty, float epsil,
+            const Dims& d, cudaStream_t s, float* info);
+
+// Diffus4th_order_core.c:44-99
+int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, float epsil,
+                const Dims& d, cudaStream_t s, float* info);
+
+// shape validation shared by every entry point
+int check_dims(int nx, int ny, int nz);
+
+}  // namespace cilreg

@@ -1,0 +1,172 @@
+// FGP-TV: Beck-Teboulle fast gradient projection on the dual of TV
+// (reference: FGP_TV_core.c:40-269, projections utils.c:149-213).
+//
+// State kept in HBM is only the dual iterates P^{k-1}, P^{k-2} (three ring
+// buffers of d components) and the data f.  The reference's R and U arrays
+// are never stored:
+//   R^{(k)} = P^{k-1} + c_{k-1} (P^{k-1} - P^{k-2}),  c_{k-1} = (t_{k-1}-1)/t_k
+//   U_k     = f - lambda * div_b R^{(k)}      (zero flux below index 0)
+//   P^k     = proj( R^{(k)} + m (U_k - U_k[+1]) )   (zero at the last index)
+// so one kernel per iteration reads P^{k-1}, P^{k-2}, f and writes P^k:
+// 40 B per voxel-iteration in 3D (28 B in 2D).  U_k is written to the output
+// only on iterations that need it (the last one, stopping checks, and the
+// iteration before a check, whose U is the check's U_prev).
+#include "drivers.cuh"
+#include "fgp_tiled.cuh"
+
+namespace cilreg {
+
+namespace {
+
+struct FgpArgs {
+    const float* pc[3];  // P^{k-1}
+    const float* po[3];  // P^{k-2}
+    float* pn[3];        // P^k (output)
+    const float* f;
+    float* u;            // U output / U_prev of the next check
+    float lam, c, multip;
+    int nonneg, aniso, write_u, write_p, check;
+};
+
+template <bool THREE>
+__device__ __forceinline__ float r_at(const FgpArgs& a, int comp, long long v) {
+    const float p = ldg(a.pc[comp], v);
+    return p + a.c * (p - ldg(a.po[comp], v));
+}
+
+// U at (i,j,k) from R (FGP_TV_core.c:220-236), then the optional clamp (:129)
+template <bool THREE>
+__device__ __forceinline__ float u_at(const FgpArgs& a, const Dims& d, int i, int j, int k) {
+    const long long v = vid(d, i, j, k);
+    const float b1 = (i == 0) ? 0.0f : r_at<THREE>(a, 0, v - 1);
+    const float b2 = (j == 0) ? 0.0f : r_at<THREE>(a, 1, v - d.nx);
+    float u;
+    if (THREE) {
+        const float b3 = (k == 0) ? 0.0f : r_at<THREE>(a, 2, v - d.sxy);
+        u = ldg(a.f, v) - a.lam * (r_at<THREE>(a, 0, v) + r_at<THREE>(a, 1, v) + r_at<THREE>(a, 2, v) - b1 - b2 - b3);
+    } else {
+        u = ldg(a.f, v) - a.lam * (r_at<THREE>(a, 0, v) + r_at<THREE>(a, 1, v) - b1 - b2);
+    }
+    if (a.nonneg && u < 0.0f) u = 0.0f;
+    return u;
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, const StopCtl* ctl,
+                                                  double2* partials) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    double pa = 0.0, pb = 0.0;
+    if (i < d.nx && j < d.ny) {
+        for (int kk = 0; kk < kz; kk++) {
+            const int k = k0 + kk;
+            if (k >= d.nz) break;
+            const long long v = vid(d, i, j, k);
+            const float u = u_at<THREE>(a, d, i, j, k);
+            if (a.check) {
+                const double df = (double)(u - a.u[v]);
+                pa += df * df;
+                pb += (double)u * (double)u;
+            }
+            if (a.write_u) a.u[v] = u;
+            if (a.write_p) {
+                // gradient step (FGP_TV_core.c:237-256)
+                const float g1 = (i == d.nx - 1) ? 0.0f : u - u_at<THREE>(a, d, i + 1, j, k);
+                const float g2 = (j == d.ny - 1) ? 0.0f : u - u_at<THREE>(a, d, i, j + 1, k);
+                float p1 = r_at<THREE>(a, 0, v) + a.multip * g1;
+                float p2 = r_at<THREE>(a, 1, v) + a.multip * g2;
+                float p3 = 0.0f;
+                if (THREE) {
+                    const float g3 = (k == d.nz - 1) ? 0.0f : u - u_at<THREE>(a, d, i, j, k + 1);
+                    p3 = r_at<THREE>(a, 2, v) + a.multip * g3;
+                }
+                // projection (utils.c:180-213)
+                if (!a.aniso) {
+                    const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
+                    if (den > 1.0f) {
+                        const float sq = 1.0f / sqrtf(den);
+                        p1 = p1 * sq;
+                        p2 = p2 * sq;
+                        p3 = p3 * sq;
+                    }
+                } else {
+                    p1 = p1 / fmaxf(fabsf(p1), 1.0f);
+                    p2 = p2 / fmaxf(fabsf(p2), 1.0f);
+                    p3 = p3 / fmaxf(fabsf(p3), 1.0f);
+                }
+                a.pn[0][v] = p1;
+                a.pn[1][v] = p2;
+                if (THREE) a.pn[2][v] = p3;
+            }
+        }
+    }
+    if (a.check) block_pair_partial<256>(pa, pb, partials, block_slot());
+}
+
+}  // namespace
+
+int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
+            const Dims& d, cudaStream_t s, float* info) {
+    const bool three = d.nz > 1;
+    const int nc = three ? 3 : 2;
+    Scratch scratch(s);
+    const Launch3 L = plan_launch(d);
+    const TiledPlan T = fgp_tiled_plan(d);
+    IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
+    CILREG_TRY(ctl.status());
+    float* ring[3][3] = {};
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < nc; c++) {
+            ring[r][c] = scratch.floats(d.n);
+            if (!ring[r][c]) return scratch.status();
+        }
+    // P^{-1} = P^{-2} = 0 (the reference's calloc'd P, P_prev, R)
+    for (int r = 1; r < 3; r++)
+        for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(ring[r][c], 0, sizeof(float) * d.n, s));
+
+    const float multip = three ? (1.0f / (12.0f * lam)) : (1.0f / (8.0f * lam));
+    float tk = 1.0f;   // t_{k}
+    float cprev = 0.0f;  // c_{k-1}; R^{(0)} = 0 whatever its value
+    int it = 0;
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        FgpArgs a;
+        for (int c = 0; c < 3; c++) {
+            a.pn[c] = ring[it % 3][c];
+            a.pc[c] = ring[(it + 2) % 3][c];
+            a.po[c] = ring[(it + 1) % 3][c];
+        }
+        a.f = f;
+        a.u = u_out;
+        a.lam = lam;
+        a.c = cprev;
+        a.multip = multip;
+        a.nonneg = (nonneg == 1);
+        a.aniso = (methodTV != 0);
+        a.check = check;
+        a.write_u = (it == iters - 1) || check || (ctl.checking() && ((it + 1) % 5 == 0));
+        a.write_p = (it != iters - 1);
+        if (T.use)
+            CILREG_TRY(fgp_tiled_step(T, a.pc, a.po, a.pn, f, u_out, lam, cprev, multip, a.nonneg, a.aniso,
+                                      a.write_u, a.write_p, check, d, ctl.ctl(), ctl.partials(), s));
+        else if (three)
+            k_fgp_step<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        else
+            k_fgp_step<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+        // t_{k+1} and the momentum coefficient for the next R (FGP_TV_core.c:138-139)
+        const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;
+        cprev = (tk - 1.0f) / tkp1;
+        tk = tkp1;
+        if (check) {
+            CILREG_TRY(ctl.after_check(it, T.use ? T.nblocks : num_blocks(L)));
+            if (ctl.host_should_stop()) break;
+        }
+    }
+    return ctl.finish(info);
+}
+
+}  // namespace cilreg

@@ -1,0 +1,172 @@
+// PD-TV: Chambolle-Pock primal-dual TV denoising (reference: PD_TV_core.c:40-252).
+//
+// One fused kernel per iteration.  State: the extrapolated primal iterate
+// Ue (the reference's U after getX) and the dual P, both ping-ponged; the
+// kernel recomputes the projected dual at the voxel and at its three lower
+// neighbours, so P never makes a second pass through HBM.  Traffic per
+// voxel-iteration: read Ue, P(3), f; write Ue, P(3) -> 36 B in 3D.
+#include "drivers.cuh"
+
+namespace cilreg {
+
+namespace {
+
+struct PdArgs {
+    const float* u;      // Ue, current
+    float* un;           // Ue, next
+    const float* p[3];   // P, current
+    float* pn[3];        // P, next
+    const float* f;
+    float* ubrk;         // U before extrapolation, written on check iterations
+    float sigma, tau, lt, onelt, theta;
+    int nonneg, aniso, check;
+};
+
+// projected dual at (i,j,k): P += sigma * mirrored forward difference of Ue
+// (PD_TV_core.c:212-229), then the projection of utils.c:180-213
+template <bool THREE>
+__device__ __forceinline__ void dual_at(const PdArgs& a, const Dims& d, int i, int j, int k, float& p1, float& p2,
+                                        float& p3) {
+    const long long v = vid(d, i, j, k);
+    const float u = ldg(a.u, v);
+    p1 = ldg(a.p[0], v) + a.sigma * (ldg(a.u, vid(d, nb_hi(i, d.nx), j, k)) - u);
+    p2 = ldg(a.p[1], v) + a.sigma * (ldg(a.u, vid(d, i, nb_hi(j, d.ny), k)) - u);
+    p3 = 0.0f;
+    if (THREE) p3 = ldg(a.p[2], v) + a.sigma * (ldg(a.u, vid(d, i, j, nb_hi(k, d.nz))) - u);
+    if (!a.aniso) {
+        const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
+        if (den > 1.0f) {
+            const float sq = 1.0f / sqrtf(den);
+            p1 *= sq;
+            p2 *= sq;
+            p3 *= sq;
+        }
+    } else {
+        p1 = p1 / fmaxf(fabsf(p1), 1.0f);
+        p2 = p2 / fmaxf(fabsf(p2), 1.0f);
+        p3 = p3 / fmaxf(fabsf(p3), 1.0f);
+    }
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_pd_step(PdArgs a, Dims d, int kz, const StopCtl* ctl, double2* partials) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    double pa = 0.0, pb = 0.0;
+    if (i < d.nx && j < d.ny) {
+        for (int kk = 0; kk < kz; kk++) {
+            const int k = k0 + kk;
+            if (k >= d.nz) break;
+            const long long v = vid(d, i, j, k);
+            float p1, p2, p3, q1, q2, q3, t1, t2, t3;
+            dual_at<THREE>(a, d, i, j, k, p1, p2, p3);
+            // backward divergence with P[-1] = 0 (PD_TV_core.c:232-252)
+            if (i == 0) q1 = -p1;
+            else { dual_at<THREE>(a, d, i - 1, j, k, t1, t2, t3); q1 = -(p1 - t1); }
+            if (j == 0) q2 = -p2;
+            else { dual_at<THREE>(a, d, i, j - 1, k, t1, t2, t3); q2 = -(p2 - t2); }
+            float dv = q1 + q2;
+            if (THREE) {
+                if (k == 0) q3 = -p3;
+                else { dual_at<THREE>(a, d, i, j, k - 1, t1, t2, t3); q3 = -(p3 - t3); }
+                dv = dv + q3;
+            }
+            float uo = ldg(a.u, v);
+            if (a.nonneg && uo < 0.0f) uo = 0.0f;  // clamp after the dual step (:120)
+            const float unew = (uo - a.tau * dv + a.lt * ldg(a.f, v)) / a.onelt;
+            if (a.check) {
+                const double df = (double)(unew - uo);
+                pa += df * df;
+                pb += (double)unew * (double)unew;
+                a.ubrk[v] = unew;
+            }
+            a.un[v] = unew + a.theta * (unew - uo);  // getX (:197-205)
+            a.pn[0][v] = p1;
+            a.pn[1][v] = p2;
+            if (THREE) a.pn[2][v] = p3;
+        }
+    }
+    if (a.check) block_pair_partial<256>(pa, pb, partials, block_slot());
+}
+
+// final output: U at the break iteration (already in dst) when stopped,
+// otherwise the extrapolated iterate of the last iteration
+__global__ void k_pd_select(const StopCtl* ctl, int iter_total, const float* b0, const float* b1, float* dst,
+                            long long n) {
+    if (ctl->stop) return;
+    const float* src = (iter_total & 1) ? b1 : b0;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+}  // namespace
+
+int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, float lipschitz, int methodTV,
+           int nonneg, const Dims& d, cudaStream_t s, float* info) {
+    const bool three = d.nz > 1;
+    const int nc = three ? 3 : 2;
+    Scratch scratch(s);
+    const Launch3 L = plan_launch(d);
+    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    CILREG_TRY(ctl.status());
+    float* ub[2];
+    float* pb[2][3] = {};
+    for (int b = 0; b < 2; b++) {
+        ub[b] = scratch.floats(d.n);
+        if (!ub[b]) return scratch.status();
+        for (int c = 0; c < nc; c++) {
+            pb[b][c] = scratch.floats(d.n);
+            if (!pb[b][c]) return scratch.status();
+        }
+    }
+    CILREG_CUDA(cudaMemcpyAsync(ub[0], f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+    for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(pb[0][c], 0, sizeof(float) * d.n, s));
+    if (iters <= 0) CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+
+    // step sizes (PD_TV_core.c:50-53): sigma = 1/(L tau) formed in double
+    const float tau = lam * 0.1f;
+    const float sigma = (float)(1.0 / (double)(lipschitz * tau));
+    const float lt = tau / lam;
+    int it = 0;
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        PdArgs a;
+        a.u = ub[it & 1];
+        a.un = ub[(it + 1) & 1];
+        for (int c = 0; c < 3; c++) {
+            a.p[c] = pb[it & 1][c];
+            a.pn[c] = pb[(it + 1) & 1][c];
+        }
+        a.f = f;
+        a.ubrk = u_out;
+        a.sigma = sigma;
+        a.tau = tau;
+        a.lt = lt;
+        a.onelt = (float)(1.0 + (double)lt);
+        a.theta = 1.0f;
+        a.nonneg = (nonneg == 1);
+        a.aniso = (methodTV != 0);
+        a.check = check;
+        if (three)
+            k_pd_step<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        else
+            k_pd_step<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+        if (check) {
+            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            if (ctl.host_should_stop()) break;
+        }
+    }
+    if (iters > 0) {
+        k_pd_select<<<1216, 256, 0, s>>>(ctl.ctl(), iters, ub[0], ub[1], u_out, d.n);
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+    }
+    return ctl.finish(info);
+}
+
+}  // namespace cilreg

@@ -1,0 +1,139 @@
+// ROF-TV explicit gradient flow (reference: ROF_TV_core.c:50-317).
+//
+// One fused kernel per iteration: the three normalised fluxes D1 (j axis),
+// D2 (i axis), D3 (k axis) are evaluated on the fly at the voxel and at its
+// mirrored lower neighbours, so neither D array is stored.  HBM traffic per
+// voxel-iteration: read U and f, write U (12 B), ping-pong U buffers.
+#include "drivers.cuh"
+
+namespace cilreg {
+
+namespace {
+
+__device__ __forceinline__ float minmod(float a, float b) {
+    return 0.5f * (sgnf(a) + sgnf(b)) * fminf(fabsf(a), fabsf(b));
+}
+
+// flux along j ("x" in the reference naming), ROF_TV_core.c:122-137
+template <bool THREE>
+__device__ __forceinline__ float flux_j(const float* __restrict__ U, const Dims& d, int i, int j, int k) {
+    const float a = ldg(U, vid(d, i, j, k));
+    const float dp = ldg(U, vid(d, i, nb_hi(j, d.ny), k)) - a;
+    const float xp = ldg(U, vid(d, nb_hi(i, d.nx), j, k)) - a;
+    const float xm = a - ldg(U, vid(d, nb_lo(i, d.nx), j, k));
+    float m = minmod(xp, xm);
+    float s = dp * dp + m * m;
+    if (THREE) {
+        const float zp = ldg(U, vid(d, i, j, nb_hi(k, d.nz))) - a;
+        const float zm = a - ldg(U, vid(d, i, j, nb_lo(k, d.nz)));
+        m = minmod(zp, zm);
+        s = s + m * m;
+    }
+    return dp / sqrtf(s + 1.0e-8f);
+}
+
+// flux along i ("y"), ROF_TV_core.c:187-200
+template <bool THREE>
+__device__ __forceinline__ float flux_i(const float* __restrict__ U, const Dims& d, int i, int j, int k) {
+    const float a = ldg(U, vid(d, i, j, k));
+    const float dp = ldg(U, vid(d, nb_hi(i, d.nx), j, k)) - a;
+    const float yp = ldg(U, vid(d, i, nb_hi(j, d.ny), k)) - a;
+    const float ym = a - ldg(U, vid(d, i, nb_lo(j, d.ny), k));
+    float m = minmod(yp, ym);
+    float s = dp * dp + m * m;
+    if (THREE) {
+        const float zp = ldg(U, vid(d, i, j, nb_hi(k, d.nz))) - a;
+        const float zm = a - ldg(U, vid(d, i, j, nb_lo(k, d.nz)));
+        m = minmod(zp, zm);
+        s = s + m * m;
+    }
+    return dp / sqrtf(s + 1.0e-8f);
+}
+
+// flux along k ("z"), ROF_TV_core.c:250-263
+__device__ __forceinline__ float flux_k(const float* __restrict__ U, const Dims& d, int i, int j, int k) {
+    const float a = ldg(U, vid(d, i, j, k));
+    const float dp = ldg(U, vid(d, i, j, nb_hi(k, d.nz))) - a;
+    const float xp = ldg(U, vid(d, nb_hi(i, d.nx), j, k)) - a;
+    const float xm = a - ldg(U, vid(d, nb_lo(i, d.nx), j, k));
+    const float yp = ldg(U, vid(d, i, nb_hi(j, d.ny), k)) - a;
+    const float ym = a - ldg(U, vid(d, i, nb_lo(j, d.ny), k));
+    const float m1 = minmod(yp, ym), m2 = minmod(xp, xm);
+    const float s = dp * dp + m1 * m1 + m2 * m2;
+    return dp / sqrtf(s + 1.0e-8f);
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_rof_step(const float* __restrict__ U, float* __restrict__ Un,
+                                                  const float* __restrict__ F, const float* __restrict__ lam_arr,
+                                                  float lam, float tau, Dims d, int kz, const StopCtl* ctl,
+                                                  int check, double2* partials) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    double pa = 0.0, pb = 0.0;
+    if (i < d.nx && j < d.ny) {
+        for (int kk = 0; kk < kz; kk++) {
+            const int k = k0 + kk;
+            if (k >= d.nz) break;
+            const long long v = vid(d, i, j, k);
+            const float u = ldg(U, v);
+            const float l = lam_arr ? ldg(lam_arr, v) : lam;
+            const float dv1 = flux_j<THREE>(U, d, i, j, k) - flux_j<THREE>(U, d, i, nb_lo(j, d.ny), k);
+            const float dv2 = flux_i<THREE>(U, d, i, j, k) - flux_i<THREE>(U, d, nb_lo(i, d.nx), j, k);
+            float div;
+            if (THREE) {
+                const float dv3 = flux_k(U, d, i, j, k) - flux_k(U, d, i, j, nb_lo(k, d.nz));
+                div = dv1 + dv2 + dv3;
+            } else {
+                div = dv1 + dv2;
+            }
+            const float un = u + tau * (l * div - (u - ldg(F, v)));
+            Un[v] = un;
+            if (check) {
+                const double df = (double)(un - u);
+                pa += df * df;
+                pb += (double)un * (double)un;
+            }
+        }
+    }
+    if (check) block_pair_partial<256>(pa, pb, partials, block_slot());
+}
+
+}  // namespace
+
+int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
+            const Dims& d, cudaStream_t s, float* info) {
+    const bool three = d.nz > 1;
+    Scratch scratch(s);
+    const Launch3 L = plan_launch(d);
+    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    CILREG_TRY(ctl.status());
+    float* alt = scratch.floats(d.n);
+    if (!alt) return scratch.status();
+    float* bufs[2] = {u_out, alt};
+    CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+    int it = 0;
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        const float* cur = bufs[it & 1];
+        float* nxt = bufs[(it + 1) & 1];
+        if (three)
+            k_rof_step<true><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl.ctl(), check,
+                                                        ctl.partials());
+        else
+            k_rof_step<false><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl.ctl(), check,
+                                                         ctl.partials());
+        CILREG_CUDA(cudaGetLastError());
+        note_launch(1);
+        if (check) {
+            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            if (ctl.host_should_stop()) break;
+        }
+    }
+    if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, bufs, u_out, d.n, s));
+    return ctl.finish(info);
+}
+
+}  // namespace cilreg

@@ -1,0 +1,276 @@
+// Host runtime: errors, devices, per-thread streams, scratch, stopping control.
+#include "runtime.cuh"
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+
+namespace cilreg {
+
+static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+int fail(int status, const char* file, int line, const char* fmt, ...) {
+    char msg[400];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof(msg), fmt, ap);
+    va_end(ap);
+    const char* base = strrchr(file, '/');
+    snprintf(g_err, sizeof(g_err), "Error: %s:%d, %s", base ? base + 1 : file, line, msg);
+    fprintf(stderr, "%s\n", g_err);
+    return status;
+}
+
+const char* last_error() { return g_err; }
+
+// ---------------------------------------------------------------------------
+static std::once_flag g_pool_once[64];
+
+int use_device(int dev) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        return fail(ERR_NODEV, __FILE__, __LINE__, "No CUDA devices found");
+    }
+    if (dev < 0 || dev >= count) {
+        return fail(ERR_ARG, __FILE__, __LINE__, "gpu_device %d out of range (0..%d)", dev, count - 1);
+    }
+    CILREG_CUDA(cudaSetDevice(dev));
+    if (dev < 64) {
+        std::call_once(g_pool_once[dev], [dev]() {
+            // keep freed scratch cached in the stream-ordered pool so that
+            // repeated calls do not remap device memory
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t thr = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            }
+        });
+    }
+    return OK;
+}
+
+cudaStream_t thread_stream(int dev) {
+    struct Streams {
+        cudaStream_t s[64] = {};
+        ~Streams() {
+            // streams die with the context at process exit; nothing to do
+        }
+    };
+    static thread_local Streams ts;
+    if (dev < 0 || dev >= 64) return 0;
+    if (!ts.s[dev]) {
+        if (cudaStreamCreateWithFlags(&ts.s[dev], cudaStreamNonBlocking) != cudaSuccess) ts.s[dev] = 0;
+    }
+    return ts.s[dev];
+}
+
+// ---------------------------------------------------------------------------
+Scratch::~Scratch() {
+    for (int i = 0; i < n_; i++)
+        if (ptrs_[i]) cudaFreeAsync(ptrs_[i], stream_);
+}
+
+void* Scratch::bytes(size_t n) {
+    if (n_ >= kMax) {
+        status_ = fail(ERR_ARG, __FILE__, __LINE__, "scratch slot table exhausted");
+        return nullptr;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, n < 64 ? 64 : n, stream_);
+    if (e != cudaSuccess) {
+        status_ = fail(e == cudaErrorMemoryAllocation ? ERR_OOM : ERR_CUDA, __FILE__, __LINE__,
+                       "scratch allocation of %zu bytes failed: %s", n, cudaGetErrorString(e));
+        return nullptr;
+    }
+    ptrs_[n_++] = p;
+    return p;
+}
+
+float* Scratch::floats(long long count) { return (float*)bytes((size_t)(count < 1 ? 1 : count) * sizeof(float)); }
+
+// ---------------------------------------------------------------------------
+__global__ void k_init_ctl(StopCtl* c, int iters) {
+    c->stop = 0;
+    c->iters = iters;
+    c->count = 0;
+    c->re = 0.0f;
+}
+
+// Deterministic reduction of the per-CTA FP64 partials, then the stopping
+// rule.  One CTA of 1024 threads; fixed assignment of partials to threads.
+__global__ void __launch_bounds__(1024) k_finalize_check(const double2* __restrict__ part, long long nparts,
+                                                          StopCtl* ctl, float epsil, int it) {
+    if (ctl->stop) return;
+    double a = 0.0, b = 0.0;
+    for (long long p = threadIdx.x; p < nparts; p += 1024) {
+        double2 v = part[p];
+        a += v.x;
+        b += v.y;
+    }
+    __shared__ double sa[32], sb[32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        a = warp_sum(sa[threadIdx.x]);
+        b = warp_sum(sb[threadIdx.x]);
+        if (threadIdx.x == 0) {
+            float re = sqrtf((float)a) / sqrtf((float)b);
+            ctl->re = re;
+            if (re < epsil) ctl->count += 1;
+            if (ctl->count > 3) {
+                ctl->stop = 1;
+                ctl->iters = it;
+            }
+        }
+    }
+}
+
+IterControl::IterControl(cudaStream_t s, Scratch& scratch, int iter_total, float epsil, long long max_partials)
+    : stream_(s), epsil_(epsil) {
+    d_ctl_ = (StopCtl*)scratch.bytes(sizeof(StopCtl));
+    if (!d_ctl_) { status_ = scratch.status(); return; }
+    if (epsil != 0.0f) {
+        d_part_ = (double2*)scratch.bytes(sizeof(double2) * (size_t)(max_partials < 1 ? 1 : max_partials));
+        if (!d_part_) { status_ = scratch.status(); return; }
+    }
+    k_init_ctl<<<1, 1, 0, s>>>(d_ctl_, iter_total);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { status_ = fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(e)); return; }
+    if (cudaMallocHost((void**)&h_ring_, sizeof(StopCtl) * 5) != cudaSuccess) {
+        status_ = fail(ERR_CUDA, __FILE__, __LINE__, "pinned allocation failed");
+        h_ring_ = nullptr;
+        return;
+    }
+    memset(h_ring_, 0, sizeof(StopCtl) * 5);
+    if (epsil != 0.0f) {
+        for (int i = 0; i < 4; i++) {
+            if (cudaEventCreateWithFlags(&ev_[i], cudaEventDisableTiming) != cudaSuccess) {
+                status_ = fail(ERR_CUDA, __FILE__, __LINE__, "event creation failed");
+                return;
+            }
+            nev_++;
+        }
+    }
+}
+
+IterControl::~IterControl() {
+    // error paths return before finish(): drain the stream before releasing
+    // the pinned mirror that pending copies may still target
+    if (h_ring_) {
+        cudaStreamSynchronize(stream_);
+        cudaFreeHost(h_ring_);
+    }
+    for (int i = 0; i < nev_; i++) cudaEventDestroy(ev_[i]);
+}
+
+int IterControl::after_check(int it, long long nparts) {
+    k_finalize_check<<<1, 1024, 0, stream_>>>(d_part_, nparts, d_ctl_, epsil_, it);
+    note_launch();
+    CILREG_CUDA(cudaGetLastError());
+    // mirror the control block to pinned memory and remember the event, so the
+    // host can stop enqueueing a few iterations after the rule fires
+    int slot = head_ % 4;
+    CILREG_CUDA(cudaMemcpyAsync(&h_ring_[slot], d_ctl_, sizeof(StopCtl), cudaMemcpyDeviceToHost, stream_));
+    CILREG_CUDA(cudaEventRecord(ev_[slot], stream_));
+    head_++;
+    if (pending_ < 4) pending_++;
+    return OK;
+}
+
+bool IterControl::host_should_stop() {
+    if (epsil_ == 0.0f || pending_ == 0) return false;
+    // keep up to two checks (about ten iterations) in flight; wait on older ones
+    while (pending_ > 2) {
+        int slot = (head_ - pending_) % 4;
+        cudaEventSynchronize(ev_[slot]);
+        pending_--;
+        if (h_ring_[slot].stop) return true;
+    }
+    int slot = (head_ - pending_) % 4;
+    if (cudaEventQuery(ev_[slot]) == cudaSuccess) {
+        pending_--;
+        if (h_ring_[slot].stop) return true;
+    }
+    return false;
+}
+
+int IterControl::finish(float* infovector, StopCtl* out) {
+    if (!h_ring_) return status_ ? status_ : ERR_CUDA;
+    CILREG_CUDA(cudaMemcpyAsync(&h_ring_[4], d_ctl_, sizeof(StopCtl), cudaMemcpyDeviceToHost, stream_));
+    CILREG_CUDA(cudaStreamSynchronize(stream_));
+    StopCtl c = h_ring_[4];
+    if (infovector) {
+        infovector[0] = (float)c.iters;
+        infovector[1] = c.re;
+    }
+    if (out) *out = c;
+    for (int i = 0; i < nev_; i++) cudaEventDestroy(ev_[i]);
+    nev_ = 0;
+    cudaFreeHost(h_ring_);
+    h_ring_ = nullptr;
+    return OK;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_fill(float* p, float v, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) p[i] = v;
+}
+
+__global__ void k_copy(float* __restrict__ d, const float* __restrict__ s, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) d[i] = s[i];
+}
+
+__global__ void k_select_copy(const StopCtl* ctl, int iter_total, const float* b0, const float* b1, float* dst,
+                              long long n) {
+    int last = ctl->stop ? ctl->iters : iter_total - 1;
+    const float* src = ((last + 1) & 1) ? b1 : b0;
+    if (src == dst) return;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+static dim3 grid_stride_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 152LL * 16) b = 152LL * 16;
+    return dim3((unsigned)(b < 1 ? 1 : b));
+}
+
+int launch_fill(float* p, float v, long long n, cudaStream_t s) {
+    k_fill<<<grid_stride_blocks(n), 256, 0, s>>>(p, v, n);
+    note_launch();
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_copy(float* dst, const float* src, long long n, cudaStream_t s) {
+    k_copy<<<grid_stride_blocks(n), 256, 0, s>>>(dst, src, n);
+    note_launch();
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_select_pingpong(const StopCtl* ctl, int iter_total, float* const bufs[2], float* dst, long long n,
+                           cudaStream_t s) {
+    k_select_copy<<<grid_stride_blocks(n), 256, 0, s>>>(ctl, iter_total, bufs[0], bufs[1], dst, n);
+    note_launch();
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+}  // namespace cilreg

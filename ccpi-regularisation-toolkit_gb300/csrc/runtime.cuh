@@ -1,0 +1,118 @@
+// Host runtime shared by all regulariser drivers: error reporting, per-thread
+// streams, stream-ordered scratch allocation and the device-side stopping
+// control.  Nothing here synchronises the device per iteration.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "common.cuh"
+
+namespace cilreg {
+
+// status codes returned through the C ABI (0 = success, negative = failure,
+// the sign convention of the reference's shared.h:15-38)
+enum Status : int {
+    OK = 0,
+    ERR_CUDA = -1,
+    ERR_ARG = -2,
+    ERR_NODEV = -3,
+    ERR_OOM = -4,
+};
+
+// record an error (thread-local message, also printed to stderr like the
+// reference's CHECK macro) and return the status
+int fail(int status, const char* file, int line, const char* fmt, ...);
+const char* last_error();
+
+#define CILREG_CUDA(call)                                                                         \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return ::cilreg::fail(e_ == cudaErrorMemoryAllocation ? ::cilreg::ERR_OOM             \
+                                                                   : ::cilreg::ERR_CUDA,          \
+                                  __FILE__, __LINE__, "code: %d, reason: %s", (int)e_,            \
+                                  cudaGetErrorString(e_));                                        \
+    } while (0)
+
+#define CILREG_TRY(expr)          \
+    do {                          \
+        int s_ = (expr);          \
+        if (s_ != 0) return s_;   \
+    } while (0)
+
+// select the device (checks that one exists) and prepare its memory pool
+int use_device(int dev);
+
+// a non-blocking stream owned by the calling host thread for device `dev`
+cudaStream_t thread_stream(int dev);
+
+// stream-ordered scratch buffers freed when the object is destroyed
+class Scratch {
+public:
+    explicit Scratch(cudaStream_t s) : stream_(s) {}
+    ~Scratch();
+    // allocate `count` floats (64-byte aligned); returns nullptr on failure
+    float* floats(long long count);
+    void* bytes(size_t n);
+    int status() const { return status_; }
+
+private:
+    static const int kMax = 48;
+    cudaStream_t stream_;
+    void* ptrs_[kMax] = {};
+    int n_ = 0;
+    int status_ = 0;
+};
+
+// Device-resident stopping control for one regulariser run.
+class IterControl {
+public:
+    IterControl(cudaStream_t s, Scratch& scratch, int iter_total, float epsil, long long max_partials);
+    ~IterControl();
+    int status() const { return status_; }
+    StopCtl* ctl() const { return d_ctl_; }
+    double2* partials() const { return d_part_; }
+    bool checking() const { return epsil_ != 0.0f; }
+    // the reference's test: a check happens at iteration `it` when it % 5 == 0
+    bool is_check(int it) const { return epsil_ != 0.0f && (it % 5) == 0; }
+    // enqueue the reduction of `nparts` partials for iteration `it`
+    int after_check(int it, long long nparts);
+    // true when the host may stop enqueueing (the rule has fired on device)
+    bool host_should_stop();
+    // wait for completion and fill infovector[0..1] (host pointer, may be null)
+    int finish(float* infovector, StopCtl* out = nullptr);
+
+private:
+    cudaStream_t stream_;
+    StopCtl* d_ctl_ = nullptr;
+    double2* d_part_ = nullptr;
+    StopCtl* h_ring_ = nullptr;  // pinned mirror slots
+    cudaEvent_t ev_[4] = {};
+    int nev_ = 0, head_ = 0, pending_ = 0;
+    float epsil_;
+    int status_ = 0;
+};
+
+// 1-D helper: grid for n elements with 256-thread CTAs
+inline dim3 grid1(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 2147483647LL) b = 2147483647LL;
+    return dim3((unsigned)(b < 1 ? 1 : b));
+}
+
+// process-wide count of kernels this library has launched (for benchmarks)
+void note_launch(long long n = 1);
+long long launch_count();
+
+// device kernels shared by the drivers (runtime.cu)
+int launch_fill(float* p, float v, long long n, cudaStream_t s);
+int launch_copy(float* dst, const float* src, long long n, cudaStream_t s);
+// copy the buffer that holds the final iterate into dst, choosing on device:
+// the last written iteration is ctl->iters when stopped, else iter_total-1;
+// buffer bufs[(last+1) & 1] holds it (ping-pong with iteration it writing bufs[(it+1)&1]).
+int launch_select_pingpong(const StopCtl* ctl, int iter_total, float* const bufs[2], float* dst, long long n,
+                           cudaStream_t s);
+
+}  // namespace cilreg

@@ -1,0 +1,181 @@
+// Split-Bregman TV (reference: SB_TV_core.c:38-371).
+//
+// Per outer iteration: two Jacobi sweeps of the (mu + 2*dim*lambda) system
+// (the reference's gauss_seidel*, which read U_prev only), then shrinkage of
+// grad U + B into D and the Bregman update of B.  Kernels:
+//   k_sb_sweep   U_out = sweep(U_in, D, B, f)        (x2, ping-pong)
+//   k_sb_shrink  D, B updated in place from the new U (one voxel each)
+// The stopping check compares the two sweeps' results (SB_TV_core.c:123-134).
+#include "drivers.cuh"
+
+namespace cilreg {
+
+namespace {
+
+struct SbArgs {
+    const float* u;   // sweep input (U_prev of the reference)
+    float* un;        // sweep output
+    const float* f;
+    float* dd[3];
+    float* bb[3];
+    float lambda, mu, norm, dlam;
+    int aniso, check;
+};
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_sb_sweep(SbArgs a, Dims d, int kz, const StopCtl* ctl, double2* partials) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    double pa = 0.0, pb = 0.0;
+    if (i < d.nx && j < d.ny) {
+        const int il = nb_lo(i, d.nx), ih = nb_hi(i, d.nx), jl = nb_lo(j, d.ny), jh = nb_hi(j, d.ny);
+        for (int kk = 0; kk < kz; kk++) {
+            const int k = k0 + kk;
+            if (k >= d.nz) break;
+            const long long v = vid(d, i, j, k);
+            const long long xi = vid(d, il, j, k), xo = vid(d, ih, j, k);
+            const long long yi = vid(d, i, jl, k), yo = vid(d, i, jh, k);
+            float sum;
+            if (THREE) {
+                const long long zi = vid(d, i, j, nb_lo(k, d.nz)), zo = vid(d, i, j, nb_hi(k, d.nz));
+                // SB_TV_core.c:273-279
+                const float dval = ldg(a.dd[0], xi) - ldg(a.dd[0], v) + ldg(a.dd[1], yi) - ldg(a.dd[1], v) +
+                                   ldg(a.dd[2], zi) - ldg(a.dd[2], v);
+                const float bval = -ldg(a.bb[0], xi) + ldg(a.bb[0], v) - ldg(a.bb[1], yi) + ldg(a.bb[1], v) -
+                                   ldg(a.bb[2], zi) + ldg(a.bb[2], v);
+                sum = dval + bval;
+                sum += ldg(a.u, xo) + ldg(a.u, xi) + ldg(a.u, yo) + ldg(a.u, yi) + ldg(a.u, zo) + ldg(a.u, zi);
+            } else {
+                // SB_TV_core.c:166-170
+                sum = ldg(a.dd[0], xi) - ldg(a.dd[0], v) + ldg(a.dd[1], yi) - ldg(a.dd[1], v) - ldg(a.bb[0], xi) +
+                      ldg(a.bb[0], v) - ldg(a.bb[1], yi) + ldg(a.bb[1], v);
+                sum += ldg(a.u, xo) + ldg(a.u, xi) + ldg(a.u, yo) + ldg(a.u, yi);
+            }
+            sum *= a.lambda;
+            sum += a.mu * ldg(a.f, v);
+            const float un = a.norm * sum;
+            a.un[v] = un;
+            if (a.check) {
+                const double df = (double)(un - ldg(a.u, v));
+                pa += df * df;
+                pb += (double)un * (double)un;
+            }
+        }
+    }
+    if (a.check) block_pair_partial<256>(pa, pb, partials, block_slot());
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_sb_shrink(SbArgs a, Dims d, int kz, const StopCtl* ctl) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    if (i >= d.nx || j >= d.ny) return;
+    const int ih = nb_hi(i, d.nx), jh = nb_hi(j, d.ny);
+    for (int kk = 0; kk < kz; kk++) {
+        const int k = k0 + kk;
+        if (k >= d.nz) break;
+        const long long v = vid(d, i, j, k);
+        const float u = ldg(a.u, v);
+        const float gx = ldg(a.u, vid(d, ih, j, k)) - u;
+        const float gy = ldg(a.u, vid(d, i, jh, k)) - u;
+        const float gz = THREE ? (ldg(a.u, vid(d, i, j, nb_hi(k, d.nz))) - u) : 0.0f;
+        const float b1 = a.bb[0][v], b2 = a.bb[1][v], b3 = THREE ? a.bb[2][v] : 0.0f;
+        const float v1 = gx + b1, v2 = gy + b2, v3 = gz + b3;
+        float d1, d2, d3 = 0.0f;
+        if (a.aniso) {
+            // SB_TV_core.c:300-310
+            const float m1 = fmaxf(fabsf(v1) - a.dlam, 0.0f);
+            const float m2 = fmaxf(fabsf(v2) - a.dlam, 0.0f);
+            d1 = (v1 != 0.0f) ? (v1 / fabsf(v1)) * m1 : 0.0f;
+            d2 = (v2 != 0.0f) ? (v2 / fabsf(v2)) * m2 : 0.0f;
+            if (THREE) {
+                const float m3 = fmaxf(fabsf(v3) - a.dlam, 0.0f);
+                d3 = (v3 != 0.0f) ? (v3 / fabsf(v3)) * m3 : 0.0f;
+            }
+        } else {
+            // SB_TV_core.c:332-349
+            const float den = THREE ? sqrtf(v1 * v1 + v2 * v2 + v3 * v3) : sqrtf(v1 * v1 + v2 * v2);
+            const float m = fmaxf(den - a.dlam, 0.0f);
+            if (den != 0.0f) {
+                d1 = m * (v1 / den);
+                d2 = m * (v2 / den);
+                d3 = m * (v3 / den);
+            } else {
+                d1 = d2 = d3 = 0.0f;
+            }
+        }
+        a.dd[0][v] = d1;
+        a.dd[1][v] = d2;
+        // Bregman update (SB_TV_core.c:366-368)
+        a.bb[0][v] = b1 + (gx - d1);
+        a.bb[1][v] = b2 + (gy - d2);
+        if (THREE) {
+            a.dd[2][v] = d3;
+            a.bb[2][v] = b3 + (gz - d3);
+        }
+    }
+}
+
+}  // namespace
+
+int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int methodTV, const Dims& d,
+           cudaStream_t s, float* info) {
+    const bool three = d.nz > 1;
+    const int nc = three ? 3 : 2;
+    Scratch scratch(s);
+    const Launch3 L = plan_launch(d);
+    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    CILREG_TRY(ctl.status());
+    float* u1 = scratch.floats(d.n);
+    if (!u1) return scratch.status();
+    SbArgs a;
+    for (int c = 0; c < 3; c++) { a.dd[c] = nullptr; a.bb[c] = nullptr; }
+    for (int c = 0; c < nc; c++) {
+        a.dd[c] = scratch.floats(d.n);
+        a.bb[c] = scratch.floats(d.n);
+        if (!a.dd[c] || !a.bb[c]) return scratch.status();
+        CILREG_CUDA(cudaMemsetAsync(a.dd[c], 0, sizeof(float) * d.n, s));
+        CILREG_CUDA(cudaMemsetAsync(a.bb[c], 0, sizeof(float) * d.n, s));
+    }
+    CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+    // mu <- 1/mu, lambda = 2 mu (SB_TV_core.c:45-46)
+    const float mu_i = 1.0f / mu;
+    a.mu = mu_i;
+    a.lambda = 2.0f * mu_i;
+    a.norm = three ? 1.0f / (a.mu + 6.0f * a.lambda) : 1.0f / (a.mu + 4.0f * a.lambda);
+    a.dlam = 1.0f / a.lambda;
+    a.aniso = (methodTV == 1);
+    a.f = f;
+    int it = 0;
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        a.check = 0;
+        a.u = u_out;
+        a.un = u1;
+        if (three) k_sb_sweep<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        else k_sb_sweep<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        CILREG_CUDA(cudaGetLastError());
+        a.check = check;
+        a.u = u1;
+        a.un = u_out;
+        if (three) k_sb_sweep<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        else k_sb_sweep<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        CILREG_CUDA(cudaGetLastError());
+        a.u = u_out;
+        if (three) k_sb_shrink<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+        else k_sb_shrink<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+        CILREG_CUDA(cudaGetLastError());
+        note_launch(3);
+        if (check) {
+            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            if (ctl.host_should_stop()) break;
+        }
+    }
+    return ctl.finish(info);
+}
+
+}  // namespace cilreg

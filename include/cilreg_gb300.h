@@ -1,0 +1,145 @@
+/*
+ * cilreg_gb300.h — C ABI of the GB300 (sm_103a) proximal regularisers.
+ *
+ * Drop-in for the CCPi Regularisation Toolkit's shared libraries:
+ *   libcilregcuda.so  exports the *_GPU_main family and the cilreg_*_dev API;
+ *   libcilreg.so      exports the *_CPU_main family (same object code).
+ * Both libraries contain all symbols below.
+ *
+ * Arrays are C-ordered float32 with dimX the fastest axis: linear index
+ * (dimX*dimY)*k + dimX*j + i.  A 2D image has dimZ == 1 (dimZ == 0 is read as 1).
+ *
+ * infovector (host pointer to 2 floats, may be NULL) receives
+ *   [iterations run (the break index when the stopping rule fired), last relative change].
+ * Stopping rule: when epsil != 0, every 5th iteration re = ||U - U_prev|| / ||U||,
+ * a counter increments when re < epsil and the run stops once it exceeds 3.
+ *
+ * Return values: 0 on success, negative on failure
+ *   -1 CUDA error, -2 invalid argument, -3 no CUDA device, -4 out of device memory;
+ * the message is available from cilreg_last_error() (per host thread) and is
+ * also printed to stderr, as the reference does (regularisers_GPU/shared.h:15-38).
+ * All entry points may be called concurrently from several host threads.
+ *
+ * Deliberate differences from the reference are listed with each function.
+ */
+#ifndef CILREG_GB300_H
+#define CILREG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Reference GPU ABI (host pointers in/out; the call copies to and from the
+ * device and returns when Output is filled).
+ * ------------------------------------------------------------------------- */
+
+/* replaces TV_ROF_GPU_main, src/Core/regularisers_GPU/headers/TV_ROF_GPU_core.h:6 */
+int TV_ROF_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, int iter, float tau,
+                    float epsil, int gpu_device, int N, int M, int Z);
+
+/* replaces TV_FGP_GPU_main, src/Core/regularisers_GPU/TV_FGP_GPU_core.h:7.
+ * As in the CPU reference, Output's initial content is U_prev of iteration 0. */
+int TV_FGP_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, int iter, float epsil,
+                    int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ);
+
+/* replaces TV_PD_GPU_main, src/Core/regularisers_GPU/headers/TV_PD_GPU_core.h:7.
+ * infovector needs 2 floats (the reference's Python passes an image-sized one). */
+int TV_PD_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, int iter, float epsil,
+                   float lipschitz_const, int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ);
+
+/* replaces TV_SB_GPU_main, src/Core/regularisers_GPU/TV_SB_GPU_core.h:8 */
+int TV_SB_GPU_main(float *Input, float *Output, float *infovector, float mu, int iter, float epsil, int methodTV,
+                   int gpu_device, int dimX, int dimY, int dimZ);
+
+/* replaces TGV_GPU_main, src/Core/regularisers_GPU/TGV_GPU_core.h:8.
+ * dimX is the fastest axis, as for every other entry point (the reference's
+ * Python passes TGV's dims reversed, src/Python/ccpi/filters/TV.py:722-725). */
+int TGV_GPU_main(float *U0, float *U, float *infovector, float lambda, float alpha1, float alpha0,
+                 int iterationsNumb, float L2, float epsil, int gpu_device, int dimX, int dimY, int dimZ);
+
+/* replaces NonlDiff_GPU_main, src/Core/regularisers_GPU/NonlDiff_GPU_core.h:6.
+ * Deterministic Jacobi sweeps (the reference updates in place, racing).
+ * penaltytype outside 1..5 with sigmaPar != 0 returns -2. */
+int NonlDiff_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                      int iterationsNumb, float tau, int penaltytype, float epsil, int gpu_device, int N, int M,
+                      int Z);
+
+/* replaces Diffus4th_GPU_main, src/Core/regularisers_GPU/Diffus_4thO_GPU_core.h:6 */
+int Diffus4th_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                       int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z);
+
+/* ---------------------------------------------------------------------------
+ * Reference C-OMP ABI.  Same argument lists and return type as the
+ * reference; the work runs on GPU CILREG_GPU_DEVICE (environment, default 0).
+ * Returns 0.0f or a negative status.
+ * ------------------------------------------------------------------------- */
+
+/* replaces TV_ROF_CPU_main, src/Core/regularisers_CPU/ROF_TV_core.h:48 (lambda_is_arr supported) */
+float TV_ROF_CPU_main(float *Input, float *Output, float *infovector, float *lambdaPar, int lambda_is_arr,
+                      int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ);
+
+/* replaces TV_FGP_CPU_main, src/Core/regularisers_CPU/FGP_TV_core.h:51 */
+float TV_FGP_CPU_main(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
+                      float epsil, int methodTV, int nonneg, int dimX, int dimY, int dimZ);
+
+/* replaces PDTV_CPU_main, src/Core/regularisers_CPU/PD_TV_core.h:50 */
+float PDTV_CPU_main(float *Input, float *U, float *infovector, float lambdaPar, int iterationsNumb, float epsil,
+                    float lipschitz_const, int methodTV, int nonneg, int dimX, int dimY, int dimZ);
+
+/* replaces SB_TV_CPU_main, src/Core/regularisers_CPU/SB_TV_core.h:48 */
+float SB_TV_CPU_main(float *Input, float *Output, float *infovector, float mu, int iter, float epsil, int methodTV,
+                     int dimX, int dimY, int dimZ);
+
+/* replaces TGV_main, src/Core/regularisers_CPU/TGV_core.h:53 */
+float TGV_main(float *U0, float *U, float *infovector, float lambda, float alpha1, float alpha0, int iter, float L2,
+               float epsil, int dimX, int dimY, int dimZ);
+
+/* replaces Diffusion_CPU_main, src/Core/regularisers_CPU/Diffusion_core.h:54 (Jacobi order) */
+float Diffusion_CPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                         int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ);
+
+/* replaces Diffus4th_CPU_main, src/Core/regularisers_CPU/Diffus4th_order_core.h:50 */
+float Diffus4th_CPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                         int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ);
+
+/* ---------------------------------------------------------------------------
+ * Device-pointer API.  d_in / d_out are distinct device buffers of
+ * dimX*dimY*dimZ floats on the current device; `stream` is a cudaStream_t
+ * (NULL = legacy default stream).  Scratch comes from the device's
+ * stream-ordered memory pool.  The call returns after the result is in d_out.
+ * These mirror the device-array API of the reference's
+ * src/Python/ccpi/filters/regularisersCuPy.py:35-40,130-138, extended to all
+ * seven regularisers; argument meanings follow the *_CPU_main lists above.
+ * ------------------------------------------------------------------------- */
+
+/* d_lambda: optional per-voxel lambda (device), overriding lambdaPar (ROF_TV_core.c:280) */
+int cilreg_rof_tv_dev(const float *d_in, float *d_out, float *infovector, const float *d_lambda, float lambdaPar,
+                      int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_fgp_tv_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, int iters, float epsil,
+                      int methodTV, int nonneg, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_pd_tv_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, int iters, float epsil,
+                     float lipschitz_const, int methodTV, int nonneg, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_sb_tv_dev(const float *d_in, float *d_out, float *infovector, float mu, int iters, float epsil,
+                     int methodTV, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_tgv_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float alpha1, float alpha0,
+                   int iters, float L2, float epsil, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_ndf_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float sigmaPar, int iters,
+                   float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_diff4th_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float sigmaPar,
+                       int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Library information (no counterpart in the reference).
+ * ------------------------------------------------------------------------- */
+const char *cilreg_last_error(void);
+const char *cilreg_version(void);
+int cilreg_device_count(void);
+/* number of kernels this library has launched in the process so far */
+long long cilreg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CILREG_GB300_H */

@@ -1,0 +1,209 @@
+"""ORACLE — TEST INFRASTRUCTURE ONLY.
+
+ctypes access to the two CPU checkers:
+
+* ``liboracle_port.so`` — the plain-C restatement in ``cilreg_port.c``; built by
+  ``make -C oracle`` on any machine (x86-64 here, aarch64 on the GPU host).
+* ``_ref/libcilreg_ref.so`` — the reference toolkit's own C-OMP sources,
+  compiled by ``make -C oracle ref`` where those sources exist.
+
+Both expose the reference's ``*_CPU_main`` argument lists
+(src/Core/regularisers_CPU/*_core.h).  Only tests, the smoke check and the
+benchmark's CPU-baseline leg import this module.  Arrays are C-ordered float32
+of shape (Z, Y, X) or (Y, X); dimX is the fastest axis, as in
+src/Python/ccpi/filters/TV.py:37-39.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_PATH = os.path.join(HERE, "liboracle_port.so")
+REF_PATH = os.path.join(HERE, "_ref", "libcilreg_ref.so")
+
+_F = ctypes.c_float
+_I = ctypes.c_int
+_P = ctypes.POINTER(ctypes.c_float)
+
+
+def build(ref: bool = True) -> None:
+    """Compile the port (and the reference, when its sources are present)."""
+    subprocess.run(["make", "-s", "-C", HERE, "ref" if ref else "all"], check=True)
+
+
+def _load(path):
+    if not os.path.exists(path):
+        return None
+    try:
+        return ctypes.CDLL(path)
+    except OSError:
+        return None
+
+
+_port = None
+_ref = None
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_PATH):
+            build(ref=False)
+        _port = _load(PORT_PATH)
+        if _port is None:
+            raise RuntimeError(f"cannot load oracle port {PORT_PATH}")
+        _declare(_port, prefix="port_")
+        _port.port_num_threads.restype = ctypes.c_int
+        _port.port_set_trace.argtypes = [_P, ctypes.c_int]
+        _port.port_trace_len.restype = ctypes.c_int
+    return _port
+
+
+def ref_lib():
+    """The compiled reference C-OMP library, or None when it is not built here."""
+    global _ref
+    if _ref is None:
+        _ref = _load(REF_PATH)
+        if _ref is not None:
+            _declare(_ref, prefix=None)
+    return _ref
+
+
+_SIGS = {
+    # name in reference, name in port, argtypes after (Input, Output, infovector)
+    "TV_ROF": ("TV_ROF_CPU_main", "port_TV_ROF", [_P, _I, _I, _F, _F]),
+    "TV_FGP": ("TV_FGP_CPU_main", "port_TV_FGP", [_F, _I, _F, _I, _I]),
+    "PDTV": ("PDTV_CPU_main", "port_PDTV", [_F, _I, _F, _F, _I, _I]),
+    "SB_TV": ("SB_TV_CPU_main", "port_SB_TV", [_F, _I, _F, _I]),
+    "TGV": ("TGV_main", "port_TGV", [_F, _F, _F, _I, _F, _F]),
+    "Diffusion": ("Diffusion_CPU_main", "port_Diffusion", [_F, _F, _I, _F, _I, _F]),
+    "Diffus4th": ("Diffus4th_CPU_main", "port_Diffus4th", [_F, _F, _I, _F, _F]),
+}
+
+
+def _declare(lib, prefix):
+    for key, (refname, portname, extra) in _SIGS.items():
+        name = portname if prefix else refname
+        fn = getattr(lib, name)
+        args = [_P, _P, _P] + extra + [_I, _I, _I]
+        if prefix and key == "Diffusion":
+            args = args + [_I]  # jacobi flag
+        fn.argtypes = args
+        fn.restype = ctypes.c_float
+
+
+def _dims(a):
+    d = list(a.shape)[::-1]
+    if a.ndim == 2:
+        d.append(1)
+    return d
+
+
+def _prep(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    out = np.zeros_like(a)
+    info = np.zeros(2, dtype=np.float32)
+    return a, out, info
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+def _lib(use_ref):
+    if use_ref:
+        lib = ref_lib()
+        if lib is None:
+            raise RuntimeError("reference C-OMP library is not built here")
+        return lib, False
+    return port_lib(), True
+
+
+def rof_tv(x, lam, iters, tau, epsil, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    lam_c = ctypes.c_float(lam)
+    fn = lib.port_TV_ROF if is_port else lib.TV_ROF_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), ctypes.byref(lam_c), 0, iters, tau, epsil, *_dims(a))
+    return out, info
+
+
+def fgp_tv(x, lam, iters, epsil, method_tv=0, nonneg=0, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_TV_FGP if is_port else lib.TV_FGP_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), lam, iters, epsil, method_tv, nonneg, *_dims(a))
+    return out, info
+
+
+def pd_tv(x, lam, iters, epsil, lipschitz=8.0, method_tv=0, nonneg=0, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_PDTV if is_port else lib.PDTV_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), lam, iters, epsil, lipschitz, method_tv, nonneg, *_dims(a))
+    return out, info
+
+
+def sb_tv(x, mu, iters, epsil, method_tv=0, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_SB_TV if is_port else lib.SB_TV_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), mu, iters, epsil, method_tv, *_dims(a))
+    return out, info
+
+
+def tgv(x, lam, alpha1, alpha0, iters, L2, epsil, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_TGV if is_port else lib.TGV_main
+    fn(_ptr(a), _ptr(out), _ptr(info), lam, alpha1, alpha0, iters, L2, epsil, *_dims(a))
+    return out, info
+
+
+def ndf(x, lam, sigma, iters, tau, penalty, epsil, jacobi=True, use_ref=False):
+    """Non-linear diffusion.  The port runs Jacobi sweeps (jacobi=True) or the
+    reference's in-place lexicographic sweep (jacobi=False, single thread)."""
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    if is_port:
+        lib.port_Diffusion(_ptr(a), _ptr(out), _ptr(info), lam, sigma, iters, tau, penalty, epsil, *_dims(a),
+                           1 if jacobi else 0)
+    else:
+        lib.Diffusion_CPU_main(_ptr(a), _ptr(out), _ptr(info), lam, sigma, iters, tau, penalty, epsil, *_dims(a))
+    return out, info
+
+
+def diff4th(x, lam, sigma, iters, tau, epsil, use_ref=False):
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_Diffus4th if is_port else lib.Diffus4th_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), lam, sigma, iters, tau, epsil, *_dims(a))
+    return out, info
+
+
+def num_threads() -> int:
+    return int(port_lib().port_num_threads())
+
+
+class trace_checks:
+    """Context manager recording every relative change the port's stopping
+    rule evaluates: ``with trace_checks() as t: ...; t.values``."""
+
+    def __init__(self, cap: int = 100000):
+        self.buf = np.zeros(cap, dtype=np.float32)
+        self.values = None
+
+    def __enter__(self):
+        port_lib().port_set_trace(_ptr(self.buf), self.buf.size)
+        return self
+
+    def __exit__(self, *exc):
+        lib = port_lib()
+        n = lib.port_trace_len()
+        lib.port_set_trace(None, 0)
+        self.values = self.buf[:n].copy()
+        return False

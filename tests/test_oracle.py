@@ -1,0 +1,96 @@
+"""CPU tests of the oracle: the C restatement must reproduce the reference's
+own C-OMP outputs (golden fixtures made by tests/golden/make_golden.py from
+the reference sources), before it is trusted as the GPU checker."""
+import platform
+
+import numpy as np
+import pytest
+
+import cases as C
+import oracle as O
+from conftest import rel_tol
+
+
+def _bit_exact_platform():
+    # the fixtures were made on x86-64; the port reproduces them bit for bit there
+    return platform.machine() in ("x86_64", "AMD64")
+
+
+@pytest.mark.parametrize("case", C.cases(), ids=lambda c: c["key"])
+def test_port_matches_reference_fixture(case, golden):
+    x = golden[f"input_{case['dim']}d"]
+    out, info = C.run_oracle(case, x, use_ref=False, jacobi=False)
+    ref = golden[f"out_{case['key']}"]
+    ref_info = golden[f"info_{case['key']}"]
+    assert out.shape == ref.shape
+    assert int(info[0]) == int(ref_info[0])
+    if _bit_exact_platform():
+        np.testing.assert_array_equal(out, ref)
+        assert info[1] == ref_info[1]
+    else:
+        assert np.max(np.abs(out - ref)) <= rel_tol(ref, 1e-6)
+
+
+def test_fixture_inputs_are_the_seeded_phantoms(golden):
+    for dim in (2, 3):
+        np.testing.assert_array_equal(C.make_input(dim), golden[f"input_{dim}d"])
+
+
+ODD_SHAPES = [(3, 5), (7, 2), (2, 3, 5), (5, 4, 3), (13, 9, 2)]
+
+
+@pytest.mark.parametrize("shape", ODD_SHAPES)
+def test_port_matches_live_reference_on_odd_shapes(shape):
+    """Against the reference compiled here (skipped where its sources are absent)."""
+    if O.ref_lib() is None:
+        pytest.skip("reference C-OMP library not built on this machine")
+    rng = np.random.default_rng(sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    checks = [
+        (O.rof_tv, (0.02, 30, 0.001, 1e-4)),
+        (O.fgp_tv, (0.05, 30, 1e-4, 0, 1)),
+        (O.pd_tv, (0.05, 30, 1e-4, 8.0, 1, 0)),
+        (O.sb_tv, (0.05, 20, 1e-4, 0)),
+        (O.tgv, (0.05, 1.0, 2.0, 30, 12.0, 1e-4)),
+        (O.diff4th, (0.8, 0.02, 30, 1e-4, 1e-4)),
+    ]
+    for fn, args in checks:
+        a, ia = fn(x, *args)
+        b, ib = fn(x, *args, use_ref=True)
+        np.testing.assert_array_equal(a, b, err_msg=fn.__name__)
+        np.testing.assert_array_equal(ia, ib, err_msg=fn.__name__)
+
+
+def test_ndf_jacobi_close_to_lexicographic():
+    """The Jacobi order (GPU semantics) and the reference's in-place order differ
+    by O(tau) per sweep; on the fixture they stay within 1e-3 of the range."""
+    x = C.make_input(2)
+    for pen in (1, 2, 3, 4, 5):
+        a, _ = O.ndf(x, 0.02, 0.05, 100, 0.01, pen, 0.0, jacobi=True)
+        b, _ = O.ndf(x, 0.02, 0.05, 100, 0.01, pen, 0.0, jacobi=False)
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-3)
+
+
+def test_trace_records_every_check():
+    x = C.make_input(2)
+    with O.trace_checks() as t:
+        _, info = O.fgp_tv(x, 0.05, 300, 3e-4, 0, 1)
+    n_checks = int(info[0]) // 5 + 1
+    assert t.values.size == n_checks
+    assert t.values[-1] == info[1]
+    assert np.sum(t.values < 3e-4) == 4  # the rule stops on the fourth hit
+
+
+def test_zero_iterations_copies_input():
+    x = C.make_input(3)
+    out, info = O.rof_tv(x, 0.02, 0, 0.001, 0.0)
+    np.testing.assert_array_equal(out, x)
+    assert info[0] == 0
+
+
+def test_invalid_penalty_rejected_by_port():
+    x = C.make_input(2)
+    lib = O.port_lib()
+    a, out, info = O._prep(x)
+    r = lib.port_Diffusion(O._ptr(a), O._ptr(out), O._ptr(info), 0.02, 0.05, 10, 0.01, 9, 0.0, *O._dims(a), 1)
+    assert r < 0
