@@ -17,6 +17,12 @@ namespace cilreg {
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info);
 
+// One ROF iteration (the kernel rof_run launches) on caller-provided buffers:
+// reads `cur`, writes `nxt`; on a check iteration writes one FP64 partial per
+// CTA (num_blocks(plan_launch(d)) of them) for launch_finalize_check.
+int rof_launch_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
+                    const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s);
+
 // FGP_TV_core.c:40-171.  u_out's initial content is U_prev of iteration 0.
 int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
             const Dims& d, cudaStream_t s, float* info);

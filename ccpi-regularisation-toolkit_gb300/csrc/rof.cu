@@ -103,6 +103,18 @@ __global__ void __launch_bounds__(256) k_rof_step(const float* __restrict__ U, f
 
 }  // namespace
 
+int rof_launch_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
+                    const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
+    const Launch3 L = plan_launch(d);
+    if (d.nz > 1)
+        k_rof_step<true><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check, partials);
+    else
+        k_rof_step<false><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check, partials);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
     const bool three = d.nz > 1;

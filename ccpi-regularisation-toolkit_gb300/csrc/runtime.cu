@@ -251,6 +251,21 @@ static dim3 grid_stride_blocks(long long n) {
     return dim3((unsigned)(b < 1 ? 1 : b));
 }
 
+int launch_init_ctl(StopCtl* ctl, int iter_total, cudaStream_t s) {
+    k_init_ctl<<<1, 1, 0, s>>>(ctl, iter_total);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
+int launch_finalize_check(const double2* partials, long long nparts, StopCtl* ctl, float epsil, int it,
+                          cudaStream_t s) {
+    k_finalize_check<<<1, 1024, 0, s>>>(partials, nparts, ctl, epsil, it);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
 int launch_fill(float* p, float v, long long n, cudaStream_t s) {
     k_fill<<<grid_stride_blocks(n), 256, 0, s>>>(p, v, n);
     note_launch();

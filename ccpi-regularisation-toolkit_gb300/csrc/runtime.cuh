@@ -107,6 +107,11 @@ void note_launch(long long n = 1);
 long long launch_count();
 
 // device kernels shared by the drivers (runtime.cu)
+// reset a StopCtl (no stop, iters = iter_total, count 0, re 0)
+int launch_init_ctl(StopCtl* ctl, int iter_total, cudaStream_t s);
+// reduce `nparts` FP64 partials and apply the stopping rule for iteration `it`
+int launch_finalize_check(const double2* partials, long long nparts, StopCtl* ctl, float epsil, int it,
+                          cudaStream_t s);
 int launch_fill(float* p, float v, long long n, cudaStream_t s);
 int launch_copy(float* dst, const float* src, long long n, cudaStream_t s);
 // copy the buffer that holds the final iterate into dst, choosing on device:

@@ -129,6 +129,21 @@ int cilreg_ndf_dev(const float *d_in, float *d_out, float *infovector, float lam
 int cilreg_diff4th_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float sigmaPar,
                        int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
 
+/* No counterpart in the reference.  ROF-TV like cilreg_rof_tv_dev, but the
+ * call allocates no device memory at all, for callers that cannot allocate
+ * when they regularise: a framework that has already claimed the GPU's memory
+ * for its own caching allocator or budget, or a real-time pipeline that
+ * forbids allocation after start-up.  Its scratch is one fixed device array
+ * of 68 MiB inside the library, held by every GPU that loads it until exit.
+ * Limits: at most 2^24 voxels (e.g. 256^3 or 4096^2), otherwise -2; with
+ * epsil != 0 at most 2^18 reduction blocks.  All calls share the array:
+ * calls whose GPU work overlaps race and must be serialised by the caller.
+ * The first call on a device looks up the array's address on that device;
+ * make it before any stream capture. */
+int cilreg_rof_tv_dev_noalloc(const float *d_in, float *d_out, float *infovector, const float *d_lambda,
+                              float lambdaPar, int iters, float tau, float epsil, int dimX, int dimY, int dimZ,
+                              void *stream);
+
 /* ---------------------------------------------------------------------------
  * Library information (no counterpart in the reference).
  * ------------------------------------------------------------------------- */
