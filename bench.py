@@ -171,6 +171,38 @@ def run_reference(args):
     return 0
 
 
+def profile_case(args):
+    """Device-only FGP calls with a fixed iteration count: the small, repeatable
+    command the committed ncu summaries were captured from."""
+    import ctypes
+
+    import torch
+    from ccpi.filters import utils as U
+
+    x = _phantom(args.size)
+    d_in = torch.from_numpy(x).cuda()
+    d_out = torch.zeros_like(d_in)
+    info = np.zeros(2, np.float32)
+    stream = torch.cuda.current_stream()
+    nx = ny = nz = args.size
+    times = []
+    for k in range(args.warmup + args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st = U.cilregcuda.cilreg_fgp_tv_dev(d_in.data_ptr(), d_out.data_ptr(),
+                                            info.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), LAM, args.iters,
+                                            0.0, METHOD, NONNEG, nx, ny, nz, stream.cuda_stream)
+        b.record(stream)
+        U.check_status(st)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            times.append(a.elapsed_time(b) / args.iters)
+    print(json.dumps({"profile_case": f"FGP_TV 3D {args.size}^3", "iters": args.iters,
+                      "ms_per_iteration": min(times)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,11 +213,16 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=4, help="iterations per reference-arm step")
     ap.add_argument("--cpu-iters", type=int, default=6, help="iterations of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
+    ap.add_argument("--iters", type=int, default=20, help="iterations per call in --profile-case")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return profile_case(args)
 
     import ctypes
 

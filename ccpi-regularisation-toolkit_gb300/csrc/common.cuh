@@ -64,12 +64,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // All threads of the block must call this (no early return before it).
+// Each thread passes FP32 sums of its own (at most a few dozen) voxels; the
+// block and grid levels add in FP64.  GB300's FP64 rate is a small fraction
+// of its FP32 rate, so per-voxel accumulation stays in FP32.
 template <int NTHREADS>
-__device__ __forceinline__ void block_pair_partial(double a, double b, double2* partials, long long slot) {
+__device__ __forceinline__ void block_pair_partial(float fa, float fb, double2* partials, long long slot) {
     __shared__ double sa[NTHREADS / 32], sb[NTHREADS / 32];
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-    a = warp_sum(a);
-    b = warp_sum(b);
+    double a = warp_sum((double)fa);
+    double b = warp_sum((double)fb);
     if ((tid & 31) == 0) { sa[tid >> 5] = a; sb[tid >> 5] = b; }
     __syncthreads();
     if (tid < 32) {

@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) k_d4_update(float* __restrict__ U, const 
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         const int im = nb_lo(i, d.nx), ip = nb_hi(i, d.nx), jm = nb_lo(j, d.ny), jp = nb_hi(j, d.ny);
         for (int kk = 0; kk < kz; kk++) {
@@ -94,9 +94,9 @@ __global__ void __launch_bounds__(256) k_d4_update(float* __restrict__ U, const 
             const float un = u + tau * (-lam * lap - (u - ldg(F, v)));
             U[v] = un;
             if (check) {
-                const double df = (double)(un - u);
+                const float df = un - u;
                 pa += df * df;
-                pb += (double)un * (double)un;
+                pb += un * un;
             }
         }
     }

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         for (int kk = 0; kk < kz; kk++) {
             const int k = k0 + kk;
@@ -66,9 +66,9 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
             const long long v = vid(d, i, j, k);
             const float u = u_at<THREE>(a, d, i, j, k);
             if (a.check) {
-                const double df = (double)(u - a.u[v]);
+                const float df = u - a.u[v];
                 pa += df * df;
-                pb += (double)u * (double)u;
+                pb += u * u;
             }
             if (a.write_u) a.u[v] = u;
             if (a.write_p) {

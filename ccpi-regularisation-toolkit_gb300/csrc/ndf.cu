@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) k_ndf_step(const float* __restrict__ U, f
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         const int il = nb_lo(i, d.nx), ih = nb_hi(i, d.nx), jl = nb_lo(j, d.ny), jh = nb_hi(j, d.ny);
         for (int kk = 0; kk < kz; kk++) {
@@ -67,9 +67,9 @@ __global__ void __launch_bounds__(256) k_ndf_step(const float* __restrict__ U, f
             const float un = c + tau * (lam * sum - (c - ldg(F, v)));
             Un[v] = un;
             if (check) {
-                const double df = (double)(un - c);
+                const float df = un - c;
                 pa += df * df;
-                pb += (double)un * (double)un;
+                pb += un * un;
             }
         }
     }

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) k_pd_step(PdArgs a, Dims d, int kz, const
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         for (int kk = 0; kk < kz; kk++) {
             const int k = k0 + kk;
@@ -77,9 +77,9 @@ __global__ void __launch_bounds__(256) k_pd_step(PdArgs a, Dims d, int kz, const
             if (a.nonneg && uo < 0.0f) uo = 0.0f;  // clamp after the dual step (:120)
             const float unew = (uo - a.tau * dv + a.lt * ldg(a.f, v)) / a.onelt;
             if (a.check) {
-                const double df = (double)(unew - uo);
+                const float df = unew - uo;
                 pa += df * df;
-                pb += (double)unew * (double)unew;
+                pb += unew * unew;
                 a.ubrk[v] = unew;
             }
             a.un[v] = unew + a.theta * (unew - uo);  // getX (:197-205)

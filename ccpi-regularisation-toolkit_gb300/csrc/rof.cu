@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) k_rof_step(const float* __restrict__ U, f
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         for (int kk = 0; kk < kz; kk++) {
             const int k = k0 + kk;
@@ -92,9 +92,9 @@ __global__ void __launch_bounds__(256) k_rof_step(const float* __restrict__ U, f
             const float un = u + tau * (l * div - (u - ldg(F, v)));
             Un[v] = un;
             if (check) {
-                const double df = (double)(un - u);
+                const float df = un - u;
                 pa += df * df;
-                pb += (double)un * (double)un;
+                pb += un * un;
             }
         }
     }

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) k_sb_sweep(SbArgs a, Dims d, int kz, cons
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         const int il = nb_lo(i, d.nx), ih = nb_hi(i, d.nx), jl = nb_lo(j, d.ny), jh = nb_hi(j, d.ny);
         for (int kk = 0; kk < kz; kk++) {
@@ -58,9 +58,9 @@ __global__ void __launch_bounds__(256) k_sb_sweep(SbArgs a, Dims d, int kz, cons
             const float un = a.norm * sum;
             a.un[v] = un;
             if (a.check) {
-                const double df = (double)(un - ldg(a.u, v));
+                const float df = un - ldg(a.u, v);
                 pa += df * df;
-                pb += (double)un * (double)un;
+                pb += un * un;
             }
         }
     }

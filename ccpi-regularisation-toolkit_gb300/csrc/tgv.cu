@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, c
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int k0 = blockIdx.z * kz;
-    double pa = 0.0, pb = 0.0;
+    float pa = 0.0f, pb = 0.0f;
     if (i < d.nx && j < d.ny) {
         for (int kk = 0; kk < kz; kk++) {
             const int k = k0 + kk;
@@ -116,9 +116,9 @@ __global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, c
             const float ue = 2.0f * un - uo;
             a.u[v] = ue;
             if (a.check) {
-                const double df = (double)(ue - uo);
+                const float df = ue - uo;
                 pa += df * df;
-                pb += (double)ue * (double)ue;
+                pb += ue * ue;
             }
             // UpdV + newV (TGV_core.c:474-533, 558-568)
             if (THREE) {

@@ -197,3 +197,20 @@ def test_fgp_512_full_size_against_port():
     out = FGP_TV(x, 0.03, 4, 0.0, 0, 1, device="gpu")
     ref, _ = O.fgp_tv(x, 0.03, 4, 0.0, 0, 1)
     assert np.max(np.abs(out - ref)) <= rel_tol(ref, TOL)
+
+
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (10, 16, 22), (67, 70, 9), (130, 33, 35)], ids=str)
+def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
+    """The 2.5D streaming FGP kernel and the per-voxel kernel compute the same iteration."""
+    from ccpi.filters.regularisers import FGP_TV
+
+    rng = np.random.default_rng(sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = FGP_TV(x, 0.05, 80, epsil, method, nonneg, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_FGP_KERNEL", "simple")
+        b = FGP_TV(x, 0.05, 80, epsil, method, nonneg, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_FGP_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
