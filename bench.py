@@ -313,7 +313,7 @@ def main():
     tpv = _ncu_traffic_per_voxel()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": (tpv * n if tpv is not None else None), "peak_kind": peak_kind,
-                "kernel": "FGP iteration (k_fgp_step)", "launch_ms": per_launch * 1e3,
+                "kernel": "FGP iteration (k_fgp_stream, csrc/fgp_tiled.cu)", "launch_ms": per_launch * 1e3,
                 "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_ITER * n}
 
     # end to end through the reference-facing C ABI with pinned host buffers
