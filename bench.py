@@ -203,6 +203,61 @@ def profile_case(args):
     return 0
 
 
+# algorithmic bytes per voxel-iteration of each regulariser's fused iteration
+SUITE_BYTES = {"ROF": (12, 12), "FGP": (40, 28), "PD": (36, 28), "SB": (60, 44), "TGV": (108, 68), "NDF": (12, 12),
+               "Diff4th": (12, 12)}
+
+
+def suite(args):
+    """Per-regulariser steady-state iteration time (difference of two fixed-count
+    runs on the same stream) on device-resident phantoms, with the roofline
+    fraction of each against the measured HBM bandwidth."""
+    import torch
+    from ccpi.filters import regularisersCuPy as D
+    from ccpi.supp.phantoms import noisy_phantom
+
+    peak, peak_kind = _peaks()
+    calls = {
+        "ROF": lambda t, n: D.ROF_TV(t, 0.02, n, 0.001),
+        "FGP": lambda t, n: D.FGP_TV(t, 0.03, n, 0.0, 0, 1),
+        "PD": lambda t, n: D.PD_TV(t, 0.03, n, 0.0, 0, 1, 8.0),
+        "SB": lambda t, n: D.SB_TV(t, 0.03, n),
+        "TGV": lambda t, n: D.TGV(t, 0.03, 1.0, 2.0, n, 12.0),
+        "NDF": lambda t, n: D.NDF(t, 0.02, 0.02, n, 0.01, 1),
+        "Diff4th": lambda t, n: D.Diff4th(t, 0.8, 0.02, n, 1e-4),
+    }
+    shapes = [(256, 256, 256), (512, 512)] if args.size <= 256 else [(args.size,) * 3, (512, 512)]
+    rows = []
+    for shape in shapes:
+        t = torch.from_numpy(noisy_phantom(shape, 30 if len(shape) == 3 else 10, 1 if len(shape) == 3 else 0)).cuda()
+        n = t.numel()
+        for name, fn in calls.items():
+            i1, i2 = (10, 40) if len(shape) == 3 else (50, 450)
+
+            def timed(iters):
+                torch.cuda.synchronize()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record()
+                fn(t, iters)
+                b.record()
+                torch.cuda.synchronize()
+                return a.elapsed_time(b) / 1e3
+
+            timed(i1)
+            t1 = min(timed(i1) for _ in range(2))
+            t2 = min(timed(i2) for _ in range(2))
+            per_it = (t2 - t1) / (i2 - i1)
+            bpv = SUITE_BYTES[name][0 if len(shape) == 3 else 1]
+            gbs = bpv * n / per_it / 1e9
+            rows.append({"regulariser": name, "shape": "x".join(map(str, shape)), "ms_per_iteration": per_it * 1e3,
+                         "voxel_iters_per_s": n / per_it, "algorithmic_bytes_per_voxel_iter": bpv,
+                         "achieved_gbs": gbs, "frac_of_hbm": gbs / peak})
+            print(json.dumps(rows[-1]))
+    print(json.dumps({"suite": rows, "peak_gbs": peak, "peak_kind": peak_kind}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -216,6 +271,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
     ap.add_argument("--iters", type=int, default=20, help="iterations per call in --profile-case")
+    ap.add_argument("--suite", action="store_true",
+                    help="per-regulariser iteration time and roofline fraction (device data, fixed counts)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -223,6 +280,8 @@ def main():
         return run_reference(args)
     if args.profile_case:
         return profile_case(args)
+    if args.suite:
+        return suite(args)
 
     import ctypes
 

@@ -22,6 +22,8 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
 // CTA (num_blocks(plan_launch(d)) of them) for launch_finalize_check.
 int rof_launch_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
                     const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s);
+// number of FP64 partial slots rof_launch_step writes on a check iteration
+long long rof_partial_slots(const Dims& d);
 
 // FGP_TV_core.c:40-171.  u_out's initial content is U_prev of iteration 0.
 int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,

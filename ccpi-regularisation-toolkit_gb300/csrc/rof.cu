@@ -5,6 +5,9 @@
 // mirrored lower neighbours, so neither D array is stored.  HBM traffic per
 // voxel-iteration: read U and f, write U (12 B), ping-pong U buffers.
 #include "drivers.cuh"
+#include "rof_tiled.cuh"
+
+#include <stdlib.h>
 
 namespace cilreg {
 
@@ -103,24 +106,40 @@ __global__ void __launch_bounds__(256) k_rof_step(const float* __restrict__ U, f
 
 }  // namespace
 
+namespace {
+// CILREG_ROF_KERNEL=simple selects the per-voxel kernel (kept for A/B checks)
+bool use_simple_kernel() {
+    const char* e = getenv("CILREG_ROF_KERNEL");
+    return e && e[0] == 's';
+}
+}  // namespace
+
+long long rof_partial_slots(const Dims& d) {
+    return use_simple_kernel() ? num_blocks(plan_launch(d)) : rof_tiled_plan(d).nblocks;
+}
+
 int rof_launch_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
                     const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
-    const Launch3 L = plan_launch(d);
-    if (d.nz > 1)
-        k_rof_step<true><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check, partials);
-    else
-        k_rof_step<false><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check, partials);
-    CILREG_CUDA(cudaGetLastError());
+    if (use_simple_kernel()) {
+        const Launch3 L = plan_launch(d);
+        if (d.nz > 1)
+            k_rof_step<true><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check, partials);
+        else
+            k_rof_step<false><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl, check,
+                                                         partials);
+        CILREG_CUDA(cudaGetLastError());
+    } else {
+        CILREG_TRY(rof_tiled_step(rof_tiled_plan(d), cur, nxt, f, lam_arr, lam, tau, d, ctl, check, partials, s));
+    }
     note_launch();
     return OK;
 }
 
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
-    const bool three = d.nz > 1;
     Scratch scratch(s);
-    const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    const long long nparts = rof_partial_slots(d);
+    IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());
     float* alt = scratch.floats(d.n);
     if (!alt) return scratch.status();
@@ -131,16 +150,9 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
         const int check = ctl.is_check(it) ? 1 : 0;
         const float* cur = bufs[it & 1];
         float* nxt = bufs[(it + 1) & 1];
-        if (three)
-            k_rof_step<true><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl.ctl(), check,
-                                                        ctl.partials());
-        else
-            k_rof_step<false><<<L.grid, L.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, L.kz, ctl.ctl(), check,
-                                                         ctl.partials());
-        CILREG_CUDA(cudaGetLastError());
-        note_launch(1);
+        CILREG_TRY(rof_launch_step(cur, nxt, f, lam_arr, lam, tau, d, ctl.ctl(), check, ctl.partials(), s));
         if (check) {
-            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            CILREG_TRY(ctl.after_check(it, nparts));
             if (ctl.host_should_stop()) break;
         }
     }

@@ -85,10 +85,9 @@ extern "C" int cilreg_rof_tv_dev_noalloc(const float* d_in, float* d_out, float*
         return fail(ERR_ARG, __FILE__, __LINE__,
                     "%lld voxels exceed the no-allocation limit of %lld voxels (use cilreg_rof_tv_dev)", d.n,
                     kNoAllocMaxVoxels);
-    const Launch3 L = plan_launch(d);
-    if (L.grid.y > 65535u || L.grid.z > 65535u)
+    if ((dimY + 7) / 8 > 65535)
         return fail(ERR_ARG, __FILE__, __LINE__, "shape (%d, %d, %d) exceeds the launch grid", dimX, dimY, dimZ);
-    const long long nparts = num_blocks(L);
+    const long long nparts = rof_partial_slots(d);
     if (epsil != 0.0f && nparts > kNoAllocMaxPartials)
         return fail(ERR_ARG, __FILE__, __LINE__,
                     "shape (%d, %d, %d) needs %lld reduction slots; the no-allocation limit is %lld", dimX, dimY,
