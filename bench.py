@@ -179,26 +179,39 @@ def profile_case(args):
     import torch
     from ccpi.filters import utils as U
 
+    from ccpi.filters import regularisersCuPy as D
+
     x = _phantom(args.size)
     d_in = torch.from_numpy(x).cuda()
     d_out = torch.zeros_like(d_in)
     info = np.zeros(2, np.float32)
     stream = torch.cuda.current_stream()
     nx = ny = nz = args.size
+    others = {
+        "ROF": lambda: D.ROF_TV(d_in, 0.02, args.iters, 0.001),
+        "PD": lambda: D.PD_TV(d_in, 0.03, args.iters, 0.0, 0, 1, 8.0),
+        "SB": lambda: D.SB_TV(d_in, 0.03, args.iters),
+        "TGV": lambda: D.TGV(d_in, 0.03, 1.0, 2.0, args.iters, 12.0),
+        "NDF": lambda: D.NDF(d_in, 0.02, 0.02, args.iters, 0.01, 1),
+        "Diff4th": lambda: D.Diff4th(d_in, 0.8, 0.02, args.iters, 1e-4),
+    }
     times = []
     for k in range(args.warmup + args.steps):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        st = U.cilregcuda.cilreg_fgp_tv_dev(d_in.data_ptr(), d_out.data_ptr(),
-                                            info.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), LAM, args.iters,
-                                            0.0, METHOD, NONNEG, nx, ny, nz, stream.cuda_stream)
+        if args.reg == "FGP":
+            st = U.cilregcuda.cilreg_fgp_tv_dev(d_in.data_ptr(), d_out.data_ptr(),
+                                                info.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), LAM, args.iters,
+                                                0.0, METHOD, NONNEG, nx, ny, nz, stream.cuda_stream)
+            U.check_status(st)
+        else:
+            others[args.reg]()
         b.record(stream)
-        U.check_status(st)
         torch.cuda.synchronize()
         if k >= args.warmup:
             times.append(a.elapsed_time(b) / args.iters)
-    print(json.dumps({"profile_case": f"FGP_TV 3D {args.size}^3", "iters": args.iters,
+    print(json.dumps({"profile_case": f"{args.reg} 3D {args.size}^3", "iters": args.iters,
                       "ms_per_iteration": min(times)}))
     return 0
 
@@ -271,6 +284,7 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
     ap.add_argument("--iters", type=int, default=20, help="iterations per call in --profile-case")
+    ap.add_argument("--reg", default="FGP", help="regulariser of --profile-case (FGP, ROF, PD, SB, TGV, NDF, Diff4th)")
     ap.add_argument("--suite", action="store_true",
                     help="per-regulariser iteration time and roofline fraction (device data, fixed counts)")
     args = ap.parse_args()

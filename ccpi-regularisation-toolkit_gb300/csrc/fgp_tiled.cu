@@ -40,18 +40,19 @@ struct TiledArgs {
     int nonneg, aniso, write_u, write_p, check;
 };
 
+// One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk.  The
+// caller reduces the returned per-thread sums when a.check is set.
 template <bool THREE>
-__global__ void __launch_bounds__(NT, 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
-                                                      double2* partials) {
+__device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& d, int zc, int bx, int by, int bz,
+                                                float& pa_out, float& pb_out) {
     __shared__ float sR1[BY][BX];
     __shared__ float sR2[BY][BX];
     __shared__ float sU[2][BY][BX];
-    if (ctl->stop) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int x = blockIdx.x * OX + tx - 1;
-    const int y = blockIdx.y * OY + ty - 1;
-    const int z0 = blockIdx.z * zc;
+    const int x = bx * OX + tx - 1;
+    const int y = by * OY + ty - 1;
+    const int z0 = bz * zc;
     const int z1 = min(z0 + zc, nz);
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
     const bool u_pt = in_xy && tx >= 1 && ty >= 1;                    // U needed here
@@ -153,16 +154,82 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream(TiledArgs a, Dims d, int z
         up = u;
         uo = uo_next;
     }
+    pa_out = pa;
+    pb_out = pb;
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(NT, 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
+                                                      double2* partials) {
+    if (ctl->stop) return;
+    float pa = 0.f, pb = 0.f;
+    fgp_stream_tile<THREE>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
     if (a.check) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
+template <bool THREE>
+__global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* __restrict__ vols,
+                                                            const int* __restrict__ tile_vol, int it, float c,
+                                                            int nonneg, int aniso, int write_u, int write_p,
+                                                            int check) {
+    const long long t = blockIdx.x;
+    const FgpBatchVol& V = vols[tile_vol[t]];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    const int bx = (int)(lt % V.gx);
+    const int by = (int)((lt / V.gx) % V.gy);
+    const int bz = (int)(lt / ((long long)V.gx * V.gy));
+    TiledArgs a;
+    for (int q = 0; q < 3; q++) {
+        a.pn[q] = V.ring[it % 3][q];
+        a.pc[q] = V.ring[(it + 2) % 3][q];
+        a.po[q] = V.ring[(it + 1) % 3][q];
+    }
+    a.f = V.f;
+    a.u = V.u;
+    a.lam = V.lam;
+    a.c = c;
+    a.multip = V.multip;
+    a.nonneg = nonneg;
+    a.aniso = aniso;
+    a.write_u = write_u;
+    a.write_p = write_p;
+    a.check = check;
+    float pa = 0.f, pb = 0.f;
+    fgp_stream_tile<THREE>(a, V.d, V.zc, bx, by, bz, pa, pb);
+    if (check) block_pair_partial<NT>(pa, pb, V.partials, lt);
+}
+
 }  // namespace
+
+void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz) {
+    gx = (d.nx + OX - 1) / OX;
+    gy = (d.ny + OY - 1) / OY;
+    gz = (d.nz + zc - 1) / zc;
+}
+
+int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int it, float c,
+                   int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s) {
+    if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    const dim3 grid((unsigned)ntiles);  // one CTA per tile of every volume
+    const dim3 block(BX, BY, 1);
+    if (three)
+        k_fgp_stream_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p,
+                                                        check);
+    else
+        k_fgp_stream_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p,
+                                                         check);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int fgp_default_zchunk(const Dims& d) { return (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1; }
 
 TiledPlan fgp_tiled_plan(const Dims& d) {
     TiledPlan T;
     const char* e = getenv("CILREG_FGP_KERNEL");
     T.use = !(e && e[0] == 's');  // "simple" selects the per-voxel kernel of fgp.cu
-    T.zchunk = (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1;
+    T.zchunk = fgp_default_zchunk(d);
     T.block = dim3(BX, BY, 1);
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;

@@ -13,9 +13,31 @@ struct TiledPlan {
 };
 
 TiledPlan fgp_tiled_plan(const Dims& d);
+int fgp_default_zchunk(const Dims& d);
 
 int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s);
+
+// One volume of a batched FGP run (device-resident descriptor table).
+struct FgpBatchVol {
+    Dims d;
+    const float* f;
+    float* u;
+    float* ring[3][3];   // three P buffers x three components
+    StopCtl* ctl;
+    double2* partials;   // this volume's slots, one per tile
+    float lam, multip;
+    long long tile_base; // first flat tile index of this volume
+    int gx, gy, gz, zc;  // tile grid and z chunk of this volume
+};
+
+// tile grid of one volume for the streaming kernel with z chunk `zc`
+void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz);
+
+// one iteration `it` of every volume: flat grid over all tiles, tile_vol maps
+// a flat tile to its volume; all volumes share dimensionality `three`
+int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int it, float c,
+                   int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s);
 
 }  // namespace cilreg

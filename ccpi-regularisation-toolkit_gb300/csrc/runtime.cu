@@ -251,6 +251,60 @@ static dim3 grid_stride_blocks(long long n) {
     return dim3((unsigned)(b < 1 ? 1 : b));
 }
 
+// one CTA per volume; the same fixed-order reduction as k_finalize_check
+__global__ void __launch_bounds__(1024) k_finalize_batch(const CheckSlot* __restrict__ slots, float epsil, int it) {
+    const CheckSlot c = slots[blockIdx.x];
+    if (c.ctl->stop) return;
+    double a = 0.0, b = 0.0;
+    for (long long p = threadIdx.x; p < c.n; p += 1024) {
+        double2 v = c.part[p];
+        a += v.x;
+        b += v.y;
+    }
+    __shared__ double sa[32], sb[32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        a = warp_sum(sa[threadIdx.x]);
+        b = warp_sum(sb[threadIdx.x]);
+        if (threadIdx.x == 0) {
+            float re = sqrtf((float)a) / sqrtf((float)b);
+            c.ctl->re = re;
+            if (re < epsil) c.ctl->count += 1;
+            if (c.ctl->count > 3) {
+                c.ctl->stop = 1;
+                c.ctl->iters = it;
+            }
+        }
+    }
+}
+
+__global__ void k_init_ctls(StopCtl* const* ctls, int nvol, int iters) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nvol) {
+        ctls[v]->stop = 0;
+        ctls[v]->iters = iters;
+        ctls[v]->count = 0;
+        ctls[v]->re = 0.0f;
+    }
+}
+
+int launch_finalize_batch(const CheckSlot* d_slots, int nvol, float epsil, int it, cudaStream_t s) {
+    k_finalize_batch<<<nvol, 1024, 0, s>>>(d_slots, epsil, it);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
+int launch_init_ctls(StopCtl* const* d_ctls, int nvol, int iter_total, cudaStream_t s) {
+    k_init_ctls<<<(nvol + 127) / 128, 128, 0, s>>>(d_ctls, nvol, iter_total);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
 int launch_init_ctl(StopCtl* ctl, int iter_total, cudaStream_t s) {
     k_init_ctl<<<1, 1, 0, s>>>(ctl, iter_total);
     CILREG_CUDA(cudaGetLastError());

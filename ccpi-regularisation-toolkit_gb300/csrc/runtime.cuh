@@ -112,6 +112,14 @@ int launch_init_ctl(StopCtl* ctl, int iter_total, cudaStream_t s);
 // reduce `nparts` FP64 partials and apply the stopping rule for iteration `it`
 int launch_finalize_check(const double2* partials, long long nparts, StopCtl* ctl, float epsil, int it,
                           cudaStream_t s);
+// per-volume stopping checks of a batch: slot v reduces part[v][0..n[v]) into ctl[v]
+struct CheckSlot {
+    const double2* part;
+    long long n;
+    StopCtl* ctl;
+};
+int launch_finalize_batch(const CheckSlot* d_slots, int nvol, float epsil, int it, cudaStream_t s);
+int launch_init_ctls(StopCtl* const* d_ctls, int nvol, int iter_total, cudaStream_t s);
 int launch_fill(float* p, float v, long long n, cudaStream_t s);
 int launch_copy(float* dst, const float* src, long long n, cudaStream_t s);
 // copy the buffer that holds the final iterate into dst, choosing on device:

@@ -8,27 +8,18 @@
 // 3D state: U, P(3), Q(6), V(3) plus U0.  The dual and primal halves of the
 // reference's ten sweeps (TGV_core.c:136-167) collapse into these two.
 #include "drivers.cuh"
+#include "tgv_batch.cuh"
 
 namespace cilreg {
 
 namespace {
 
-struct TgvArgs {
-    float* u;
-    const float* u0;
-    float* p[3];
-    float* q[6];
-    float* v[3];
-    float lambda, alpha1, alpha0, tau, sigma;
-    int check;
-};
 
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_dual(TgvArgs a, Dims d, int kz, const StopCtl* ctl) {
-    if (ctl->stop) return;
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int k0 = blockIdx.z * kz;
+__device__ __forceinline__ void tgv_dual_tile(const TgvArgs& a, const Dims& d, int kz, int bx, int by, int bz) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k0 = bz * kz;
     if (i >= d.nx || j >= d.ny) return;
     const bool xe = (i == d.nx - 1), ye = (j == d.ny - 1);
     for (int kk = 0; kk < kz; kk++) {
@@ -88,6 +79,12 @@ __global__ void __launch_bounds__(256) k_tgv_dual(TgvArgs a, Dims d, int kz, con
     }
 }
 
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_tgv_dual(TgvArgs a, Dims d, int kz, const StopCtl* ctl) {
+    if (ctl->stop) return;
+    tgv_dual_tile<THREE>(a, d, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // backward difference with the reference's three-case boundary (TGV_core.c:286-292)
 __device__ __forceinline__ float bwd(const float* X, long long v, long long stride, int i, int n) {
     if (i == 0) return X[v];
@@ -96,13 +93,11 @@ __device__ __forceinline__ float bwd(const float* X, long long v, long long stri
 }
 
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, const StopCtl* ctl,
-                                                    double2* partials) {
-    if (ctl->stop) return;
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int k0 = blockIdx.z * kz;
-    float pa = 0.0f, pb = 0.0f;
+__device__ __forceinline__ void tgv_primal_tile(const TgvArgs& a, const Dims& d, int kz, int bx, int by, int bz,
+                                                float& pa, float& pb) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k0 = bz * kz;
     if (i < d.nx && j < d.ny) {
         for (int kk = 0; kk < kz; kk++) {
             const int k = k0 + kk;
@@ -143,10 +138,61 @@ __global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, c
             }
         }
     }
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, const StopCtl* ctl,
+                                                    double2* partials) {
+    if (ctl->stop) return;
+    float pa = 0.0f, pb = 0.0f;
+    tgv_primal_tile<THREE>(a, d, kz, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
     if (a.check) block_pair_partial<256>(pa, pb, partials, block_slot());
 }
 
+// batched: one flat grid over the tiles of every volume
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_tgv_dual_batch(const TgvBatchVol* __restrict__ vols,
+                                                        const int* __restrict__ tile_vol) {
+    const long long t = blockIdx.x;
+    const TgvBatchVol& V = vols[tile_vol[t]];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    TgvArgs a = V.args;
+    tgv_dual_tile<THREE>(a, V.d, V.kz, (int)(lt % V.gx), (int)((lt / V.gx) % V.gy),
+                         (int)(lt / ((long long)V.gx * V.gy)));
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_tgv_primal_batch(const TgvBatchVol* __restrict__ vols,
+                                                          const int* __restrict__ tile_vol, int check) {
+    const long long t = blockIdx.x;
+    const TgvBatchVol& V = vols[tile_vol[t]];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    TgvArgs a = V.args;
+    a.check = check;
+    float pa = 0.0f, pb = 0.0f;
+    tgv_primal_tile<THREE>(a, V.d, V.kz, (int)(lt % V.gx), (int)((lt / V.gx) % V.gy),
+                           (int)(lt / ((long long)V.gx * V.gy)), pa, pb);
+    if (check) block_pair_partial<256>(pa, pb, V.partials, lt);
+}
+
 }  // namespace
+
+int tgv_batch_step(const TgvBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int check,
+                   cudaStream_t s) {
+    if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    const dim3 grid((unsigned)ntiles), block(32, 8, 1);
+    if (three) {
+        k_tgv_dual_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
+        k_tgv_primal_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
+    } else {
+        k_tgv_dual_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
+        k_tgv_primal_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
+    }
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
 
 int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2, float epsil,
             const Dims& d, cudaStream_t s, float* info) {

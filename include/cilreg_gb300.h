@@ -129,6 +129,27 @@ int cilreg_ndf_dev(const float *d_in, float *d_out, float *infovector, float lam
 int cilreg_diff4th_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float sigmaPar,
                        int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched API (no counterpart in the reference, whose callers loop over
+ * volumes, e.g. demos/multi_gpu.py).  nvol volumes of any shapes (all 2D or
+ * all 3D): d_in/d_out are host arrays of nvol device pointers, dims holds
+ * (dimX, dimY, dimZ) per volume, lambdas one value per volume, infovectors
+ * (host, may be NULL) 2 floats per volume.  Every volume follows its own
+ * stopping rule.  All volumes advance together: one kernel launch per
+ * iteration over all volumes' tiles, and by default the whole iteration loop
+ * is one CUDA graph launch (CILREG_BATCH_GRAPH=0 disables the graph;
+ * CILREG_BATCH_AUTOTUNE=1 times candidate z chunks of the FGP kernel on the
+ * batch and keeps the choice, also in the file CILREG_AUTOTUNE_CACHE).  The
+ * call returns when every output is written.  Results equal those of the
+ * single-volume calls (FGP bit for bit, TGV to the last bits).
+ * ------------------------------------------------------------------------- */
+int cilreg_fgp_tv_batch_dev(int nvol, const float *const *d_in, float *const *d_out, const int *dims,
+                            const float *lambdas, int iters, float epsil, int methodTV, int nonneg, float *infovectors,
+                            void *stream);
+int cilreg_tgv_batch_dev(int nvol, const float *const *d_in, float *const *d_out, const int *dims,
+                         const float *lambdas, float alpha1, float alpha0, int iters, float L2, float epsil,
+                         float *infovectors, void *stream);
+
 /* No counterpart in the reference.  ROF-TV like cilreg_rof_tv_dev, but the
  * call allocates no device memory at all, for callers that cannot allocate
  * when they regularise: a framework that has already claimed the GPU's memory
