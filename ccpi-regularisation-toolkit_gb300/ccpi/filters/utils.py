@@ -62,6 +62,9 @@ _DEV_SIGS = {
 
 _PP = ctypes.POINTER(ctypes.c_void_p)
 _IP = ctypes.POINTER(ctypes.c_int)
+_VJP_SIGS = {
+    "cilreg_fgp_tv_vjp_dev": [_V, _V, _V, ctypes.POINTER(ctypes.c_double), _F, _I, _I, _I, _I, _I, _I, _I, _V],
+}
 _BATCH_SIGS = {
     "cilreg_fgp_tv_batch_dev": [_I, _PP, _PP, _IP, _P, _I, _F, _I, _I, _P, _V],
     "cilreg_tgv_batch_dev": [_I, _PP, _PP, _IP, _P, _F, _F, _I, _F, _F, _P, _V],
@@ -71,7 +74,7 @@ for _lib in (cilreg, cilregcuda):
     for _name, _args in _CPU_SIGS.items():
         getattr(_lib, _name).argtypes = _args
         getattr(_lib, _name).restype = ctypes.c_float
-    for _name, _args in {**_GPU_SIGS, **_DEV_SIGS, **_BATCH_SIGS}.items():
+    for _name, _args in {**_GPU_SIGS, **_DEV_SIGS, **_BATCH_SIGS, **_VJP_SIGS}.items():
         getattr(_lib, _name).argtypes = _args
         getattr(_lib, _name).restype = ctypes.c_int
     _lib.cilreg_last_error.restype = ctypes.c_char_p

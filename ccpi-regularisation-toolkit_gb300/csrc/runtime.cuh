@@ -59,7 +59,7 @@ public:
     int status() const { return status_; }
 
 private:
-    static const int kMax = 48;
+    static const int kMax = 1024;
     cudaStream_t stream_;
     void* ptrs_[kMax] = {};
     int n_ = 0;

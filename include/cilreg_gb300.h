@@ -150,6 +150,18 @@ int cilreg_tgv_batch_dev(int nvol, const float *const *d_in, float *const *d_out
                          const float *lambdas, float alpha1, float alpha0, int iters, float L2, float epsil,
                          float *infovectors, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiation (no counterpart in the reference).  Vector-Jacobian product
+ * of the unrolled FGP-TV map y = FGP(f, lambda) with `iters` iterations and no
+ * stopping rule (the map cilreg_fgp_tv_dev computes with epsil = 0): given
+ * d_ybar = dL/dy it writes d_inbar = dL/df (device) and *lambar = dL/dlambda
+ * (host).  Forward states are stored every `checkpoint` iterations (1..64) and
+ * each segment is recomputed before its reverse sweep.
+ * ------------------------------------------------------------------------- */
+int cilreg_fgp_tv_vjp_dev(const float *d_in, const float *d_ybar, float *d_inbar, double *lambar, float lambdaPar,
+                          int iters, int methodTV, int nonneg, int checkpoint, int dimX, int dimY, int dimZ,
+                          void *stream);
+
 /* No counterpart in the reference.  ROF-TV like cilreg_rof_tv_dev, but the
  * call allocates no device memory at all, for callers that cannot allocate
  * when they regularise: a framework that has already claimed the GPU's memory
