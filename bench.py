@@ -362,6 +362,48 @@ def autograd_bench(args):
     return 0
 
 
+def serve_requests(n, seed=3, rate=200.0):
+    """The served workload: Poisson arrivals (mean `rate`/s), half 2D 1024^2,
+    half 3D with edges from 128 to 384 (step 32); ROF / FGP / SB / NDF(Huber,
+    sigma 0.02) uniformly; 5-50 outer FISTA steps of 20 inner iterations."""
+    from ccpi.filters.serving import ProxRequest
+    from ccpi.supp.phantoms import noisy_phantom
+
+    rng = np.random.default_rng(seed)
+    algs = [("ROF", (0.02, 0.001)), ("FGP", (0.03, 0, 1)), ("SB", (0.03, 0)), ("NDF", (0.02, 0.02, 0.01, 1))]
+    cache = {}
+    reqs, t = [], 0.0
+    for i in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        if rng.random() < 0.5:
+            shape = (1024, 1024)
+        else:
+            e = int(rng.choice(np.arange(128, 385, 32)))
+            shape = (e, e, e)
+        if shape not in cache:  # one phantom per size class, reused
+            cache[shape] = noisy_phantom(shape, 30 if len(shape) == 3 else 10, 3)
+        alg, prm = algs[int(rng.integers(0, 4))]
+        reqs.append(ProxRequest(i, alg, cache[shape], prm, outer=int(rng.integers(5, 51)), inner=20, arrival=t))
+    return reqs
+
+
+def serve_bench(args):
+    from ccpi.filters.serving import ProxServer, summarise
+
+    reqs = serve_requests(args.requests)
+    server = ProxServer(slots=8, hbm_budget=150e9)
+    server.serve(reqs[:4], realtime=False)  # warm-up: module load, pool growth
+    t = time.perf_counter()
+    res = server.serve(reqs)
+    wall = time.perf_counter() - t
+    out = summarise(res, wall)
+    out["workload"] = (f"{len(reqs)} prox requests, Poisson mean 200/s, 2D 1024^2 / 3D 128^3-384^3, "
+                       "ROF/FGP/SB/NDF, 5-50 FISTA steps x 20 inner iterations, 8 slots, 150 GB budget")
+    out["volumes_per_s"] = out["requests_per_s"]
+    print(json.dumps({"serve": out}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,6 +422,9 @@ def main():
                     help="64 uneven volumes, FGP and TGV at 300 iterations: batched graph launch vs per-call")
     ap.add_argument("--autograd", action="store_true",
                     help="unrolled FGP-TV forward + adjoint on 8 volumes of 128^3, 200 iterations, checkpoint 20")
+    ap.add_argument("--serve", action="store_true",
+                    help="Poisson stream (mean 200 req/s) of prox requests through the continuous-batching server")
+    ap.add_argument("--requests", type=int, default=48, help="requests of the --serve stream")
     ap.add_argument("--suite", action="store_true",
                     help="per-regulariser iteration time and roofline fraction (device data, fixed counts)")
     args = ap.parse_args()
@@ -395,6 +440,8 @@ def main():
         return batch_bench(args)
     if args.autograd:
         return autograd_bench(args)
+    if args.serve:
+        return serve_bench(args)
 
     import ctypes
 

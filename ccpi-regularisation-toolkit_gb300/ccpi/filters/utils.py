@@ -65,6 +65,12 @@ _IP = ctypes.POINTER(ctypes.c_int)
 _VJP_SIGS = {
     "cilreg_fgp_tv_vjp_dev": [_V, _V, _V, ctypes.POINTER(ctypes.c_double), _F, _I, _I, _I, _I, _I, _I, _I, _V],
 }
+_SESSION_SIGS = {
+    "cilreg_prox_session_create": [ctypes.POINTER(ctypes.c_void_p), _I, _P, _I, _I, _I, _I, _V],
+    "cilreg_prox_session_prox": [_V, _V, _V, _I, _F, _P, _V],
+    "cilreg_prox_session_fista": [_V, _V, _V, _I, _I, _F, _V],
+    "cilreg_prox_session_destroy": [_V, _V],
+}
 _BATCH_SIGS = {
     "cilreg_fgp_tv_batch_dev": [_I, _PP, _PP, _IP, _P, _I, _F, _I, _I, _P, _V],
     "cilreg_tgv_batch_dev": [_I, _PP, _PP, _IP, _P, _F, _F, _I, _F, _F, _P, _V],
@@ -74,13 +80,15 @@ for _lib in (cilreg, cilregcuda):
     for _name, _args in _CPU_SIGS.items():
         getattr(_lib, _name).argtypes = _args
         getattr(_lib, _name).restype = ctypes.c_float
-    for _name, _args in {**_GPU_SIGS, **_DEV_SIGS, **_BATCH_SIGS, **_VJP_SIGS}.items():
+    for _name, _args in {**_GPU_SIGS, **_DEV_SIGS, **_BATCH_SIGS, **_VJP_SIGS, **_SESSION_SIGS}.items():
         getattr(_lib, _name).argtypes = _args
         getattr(_lib, _name).restype = ctypes.c_int
     _lib.cilreg_last_error.restype = ctypes.c_char_p
     _lib.cilreg_version.restype = ctypes.c_char_p
     _lib.cilreg_device_count.restype = ctypes.c_int
     _lib.cilreg_launch_count.restype = ctypes.c_longlong
+    _lib.cilreg_prox_session_bytes.argtypes = [_I, _I, _I, _I]
+    _lib.cilreg_prox_session_bytes.restype = ctypes.c_longlong
 
 
 class RegulariserError(RuntimeError):

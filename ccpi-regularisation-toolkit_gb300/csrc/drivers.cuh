@@ -13,9 +13,21 @@
 
 namespace cilreg {
 
+// Device state a regulariser keeps between calls (warm start across the outer
+// iterations of a proximal-splitting solver).  Owned by the caller.
+struct FgpWarm {
+    float* ring[3][3];  // the three dual buffers (P_{k-1}, P_{k-2}, P_k)
+    int base;           // ring index offset: iteration it writes ring[(base + it) % 3]
+};
+struct SbWarm {
+    float* dd[3];  // D (split variable)
+    float* bb[3];  // B (Bregman variable)
+};
+
 // ROF_TV_core.c:50-99.  lam_arr (device, per voxel) overrides lam when non-null.
+// u_init (device, optional) replaces f as the starting iterate
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
-            const Dims& d, cudaStream_t s, float* info);
+            const Dims& d, cudaStream_t s, float* info, const float* u_init = nullptr);
 
 // One ROF iteration (the kernel rof_run launches) on caller-provided buffers:
 // reads `cur`, writes `nxt`; on a check iteration writes one FP64 partial per
@@ -26,24 +38,27 @@ int rof_launch_step(const float* cur, float* nxt, const float* f, const float* l
 long long rof_partial_slots(const Dims& d);
 
 // FGP_TV_core.c:40-171.  u_out's initial content is U_prev of iteration 0.
+// warm (optional): dual state carried across calls; its ring is updated
 int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
-            const Dims& d, cudaStream_t s, float* info);
+            const Dims& d, cudaStream_t s, float* info, FgpWarm* warm = nullptr);
 
 // PD_TV_core.c:40-153
 int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, float lipschitz, int methodTV,
            int nonneg, const Dims& d, cudaStream_t s, float* info);
 
 // SB_TV_core.c:38-144
+// warm (optional): D and B carried across calls
 int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int methodTV, const Dims& d,
-           cudaStream_t s, float* info);
+           cudaStream_t s, float* info, SbWarm* warm = nullptr);
 
 // TGV_core.c:43-194
 int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2, float epsil,
             const Dims& d, cudaStream_t s, float* info);
 
 // Diffusion_core.c:53-102, Jacobi update order
+// u_init (device, optional) replaces f as the starting iterate
 int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, int penalty, float epsil,
-            const Dims& d, cudaStream_t s, float* info);
+            const Dims& d, cudaStream_t s, float* info, const float* u_init = nullptr);
 
 // Diffus4th_order_core.c:44-99
 int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, float epsil,

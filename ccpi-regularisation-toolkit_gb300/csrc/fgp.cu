@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
 }  // namespace
 
 int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
-            const Dims& d, cudaStream_t s, float* info) {
+            const Dims& d, cudaStream_t s, float* info, FgpWarm* warm) {
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
@@ -117,14 +117,22 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
     CILREG_TRY(ctl.status());
     float* ring[3][3] = {};
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < nc; c++) {
-            ring[r][c] = scratch.floats(d.n);
-            if (!ring[r][c]) return scratch.status();
-        }
-    // P^{-1} = P^{-2} = 0 (the reference's calloc'd P, P_prev, R)
-    for (int r = 1; r < 3; r++)
-        for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(ring[r][c], 0, sizeof(float) * d.n, s));
+    int base = 0;
+    if (warm) {
+        // warm start: the caller's dual buffers hold P_{-1}, P_{-2} of this call
+        base = warm->base;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) ring[r][c] = warm->ring[(base + r) % 3][c];
+    } else {
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < nc; c++) {
+                ring[r][c] = scratch.floats(d.n);
+                if (!ring[r][c]) return scratch.status();
+            }
+        // P^{-1} = P^{-2} = 0 (the reference's calloc'd P, P_prev, R)
+        for (int r = 1; r < 3; r++)
+            for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(ring[r][c], 0, sizeof(float) * d.n, s));
+    }
 
     const float multip = three ? (1.0f / (12.0f * lam)) : (1.0f / (8.0f * lam));
     float tk = 1.0f;   // t_{k}
@@ -147,7 +155,7 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         a.aniso = (methodTV != 0);
         a.check = check;
         a.write_u = (it == iters - 1) || check || (ctl.checking() && ((it + 1) % 5 == 0));
-        a.write_p = (it != iters - 1);
+        a.write_p = (it != iters - 1) || warm;  // a warm state keeps the last dual iterate
         if (T.use)
             CILREG_TRY(fgp_tiled_step(T, a.pc, a.po, a.pn, f, u_out, lam, cprev, multip, a.nonneg, a.aniso,
                                       a.write_u, a.write_p, check, d, ctl.ctl(), ctl.partials(), s));
@@ -166,7 +174,14 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
             if (ctl.host_should_stop()) break;
         }
     }
-    return ctl.finish(info);
+    StopCtl done;
+    CILREG_TRY(ctl.finish(info, &done));
+    if (warm) {
+        // iterations 0..last wrote ring[(base + it) % 3]
+        const int ran = done.stop ? done.iters + 1 : iters;
+        warm->base = (base + ran) % 3;
+    }
+    return OK;
 }
 
 }  // namespace cilreg

@@ -98,7 +98,7 @@ void launch_ndf(int pen, const Launch3& L, cudaStream_t s, const float* U, float
 }  // namespace
 
 int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, int penalty, float epsil,
-            const Dims& d, cudaStream_t s, float* info) {
+            const Dims& d, cudaStream_t s, float* info, const float* u_init) {
     const bool linear = (sigma == 0.0f);
     if (!linear && (penalty < 1 || penalty > 5))
         return fail(ERR_ARG, __FILE__, __LINE__, "No penalty function selected! Use 1,2,3,4 or 5.");
@@ -112,7 +112,7 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     float* alt = scratch.floats(d.n);
     if (!alt) return scratch.status();
     float* bufs[2] = {u_out, alt};
-    CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;

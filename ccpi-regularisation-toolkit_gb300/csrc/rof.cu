@@ -136,7 +136,7 @@ int rof_launch_step(const float* cur, float* nxt, const float* f, const float* l
 }
 
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
-            const Dims& d, cudaStream_t s, float* info) {
+            const Dims& d, cudaStream_t s, float* info, const float* u_init) {
     Scratch scratch(s);
     const long long nparts = rof_partial_slots(d);
     IterControl ctl(s, scratch, iters, epsil, nparts);
@@ -144,7 +144,7 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
     float* alt = scratch.floats(d.n);
     if (!alt) return scratch.status();
     float* bufs[2] = {u_out, alt};
-    CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;

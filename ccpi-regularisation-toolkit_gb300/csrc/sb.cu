@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_sb_shrink(SbArgs a, Dims d, int kz, con
 }  // namespace
 
 int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int methodTV, const Dims& d,
-           cudaStream_t s, float* info) {
+           cudaStream_t s, float* info, SbWarm* warm) {
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
@@ -135,6 +135,11 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
     SbArgs a;
     for (int c = 0; c < 3; c++) { a.dd[c] = nullptr; a.bb[c] = nullptr; }
     for (int c = 0; c < nc; c++) {
+        if (warm) {
+            a.dd[c] = warm->dd[c];
+            a.bb[c] = warm->bb[c];
+            continue;
+        }
         a.dd[c] = scratch.floats(d.n);
         a.bb[c] = scratch.floats(d.n);
         if (!a.dd[c] || !a.bb[c]) return scratch.status();

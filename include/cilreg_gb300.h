@@ -162,6 +162,31 @@ int cilreg_fgp_tv_vjp_dev(const float *d_in, const float *d_ybar, float *d_inbar
                           int iters, int methodTV, int nonneg, int checkpoint, int dimX, int dimY, int dimZ,
                           void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Prox sessions (no counterpart in the reference, which discards all state at
+ * the end of every call).  A session holds a regulariser's state on the
+ * device across the outer iterations of a proximal-splitting solver:
+ *   alg 0 ROF-TV  params {lambda, tau}            keeps the previous prox output
+ *   alg 1 FGP-TV  params {lambda, methodTV, nonneg} keeps the dual iterates P
+ *   alg 2 SB-TV   params {mu, methodTV}           keeps the split/Bregman D, B
+ *   alg 3 NDF     params {lambda, sigma, tau, penalty} keeps the previous output
+ * cilreg_prox_session_bytes gives the device memory one session needs (state
+ * plus the transient scratch of a prox call), for admission control.
+ * _prox runs `iters` warm-started iterations of the regulariser on d_in;
+ * _fista solves min_x 1/2 ||x - f||^2 + R(x) with `outer` FISTA steps of
+ * gradient step `step`, each prox being `inner` warm-started iterations, and
+ * writes x to d_x.  A session is used by one host thread at a time.
+ * ------------------------------------------------------------------------- */
+typedef struct cilreg_session cilreg_session;
+long long cilreg_prox_session_bytes(int alg, int dimX, int dimY, int dimZ);
+int cilreg_prox_session_create(cilreg_session **session, int alg, const float *params, int nparams, int dimX,
+                               int dimY, int dimZ, void *stream);
+int cilreg_prox_session_prox(cilreg_session *session, const float *d_in, float *d_out, int iters, float epsil,
+                             float *infovector, void *stream);
+int cilreg_prox_session_fista(cilreg_session *session, const float *d_f, float *d_x, int outer, int inner, float step,
+                              void *stream);
+int cilreg_prox_session_destroy(cilreg_session *session, void *stream);
+
 /* No counterpart in the reference.  ROF-TV like cilreg_rof_tv_dev, but the
  * call allocates no device memory at all, for callers that cannot allocate
  * when they regularise: a framework that has already claimed the GPU's memory
