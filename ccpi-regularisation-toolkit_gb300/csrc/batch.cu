@@ -376,6 +376,7 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
         a.alpha0 = alpha0;
         a.tau = tau;
         a.sigma = tau;
+        a.inv_lt = 1.0f / (a.lambda + tau);
         a.check = 0;
         V.ctl = d_ctl + v;
         V.partials = part + V.tile_base;

@@ -11,7 +11,7 @@ namespace cilreg {
 namespace {
 
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_d4_laplacian(const float* __restrict__ U, float* __restrict__ W, float sg2,
+__global__ void __launch_bounds__(256) k_d4_laplacian(const float* __restrict__ U, float* __restrict__ W, float isg2,
                                                       Dims d, int kz, const StopCtl* ctl) {
     if (ctl->stop) return;
     const int i = blockIdx.x * 32 + threadIdx.x;
@@ -51,18 +51,18 @@ __global__ void __launch_bounds__(256) k_d4_laplacian(const float* __restrict__ 
             den = gx2 + gy2 + gz2;
             const float nn = gxx * gx2 + gyy * gy2 + gzz * gz2 + xy2 + xz2 + yz2;
             const float oo = (gy2 + gz2) * gxx + (gx2 + gz2) * gyy + (gx2 + gy2) * gzz - xy2 - xz2 - yz2;
-            const float q = (den <= EPS) ? EPS : den;
-            vn = nn / q;
-            vo = oo / q;
+            const float iq = __frcp_rn((den <= EPS) ? EPS : den);  // one reciprocal for both quotients
+            vn = nn * iq;
+            vo = oo * iq;
         } else {
             den = gx2 + gy2;
             const float nn = gxx * gx2 + xy2 + gyy * gy2;
             const float oo = gxx * gy2 - xy2 + gyy * gx2;
-            const float q = (den <= EPS) ? EPS : den;
-            vn = nn / q;
-            vo = oo / q;
+            const float iq = __frcp_rn((den <= EPS) ? EPS : den);
+            vn = nn * iq;
+            vo = oo * iq;
         }
-        const float c = 1.0f / (1.0f + den / sg2);
+        const float c = __frcp_rn(1.0f + den * isg2);
         W[v] = (c * c) * vn + c * vo;
     }
 }
@@ -116,15 +116,16 @@ int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters,
     if (!W) return scratch.status();
     CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     const float sg2 = sigma * sigma;  // Diffus4th_order_core.c:51
+    const float isg2 = 1.0f / sg2;    // den / sg2 formed as den * isg2 (within 1 ulp)
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         if (three) {
-            k_d4_laplacian<true><<<L.grid, L.block, 0, s>>>(u_out, W, sg2, d, L.kz, ctl.ctl());
+            k_d4_laplacian<true><<<L.grid, L.block, 0, s>>>(u_out, W, isg2, d, L.kz, ctl.ctl());
             k_d4_update<true><<<L.grid, L.block, 0, s>>>(u_out, W, f, lam, tau, d, L.kz, ctl.ctl(), check,
                                                          ctl.partials());
         } else {
-            k_d4_laplacian<false><<<L.grid, L.block, 0, s>>>(u_out, W, sg2, d, L.kz, ctl.ctl());
+            k_d4_laplacian<false><<<L.grid, L.block, 0, s>>>(u_out, W, isg2, d, L.kz, ctl.ctl());
             k_d4_update<false><<<L.grid, L.block, 0, s>>>(u_out, W, f, lam, tau, d, L.kz, ctl.ctl(), check,
                                                           ctl.partials());
         }

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
                 if (!a.aniso) {
                     const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
                     if (den > 1.0f) {
-                        const float sq = 1.0f / sqrtf(den);
+                        const float sq = rsqrtf(den);  // within 2 ulp of 1/sqrtf
                         p1 = p1 * sq;
                         p2 = p2 * sq;
                         p3 = p3 * sq;

@@ -133,7 +133,7 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
                 if (!a.aniso) {
                     const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
                     if (den > 1.f) {
-                        const float sq = 1.f / sqrtf(den);
+                        const float sq = rsqrtf(den);  // within 2 ulp of 1/sqrtf
                         p1 = p1 * sq;
                         p2 = p2 * sq;
                         p3 = p3 * sq;

@@ -36,7 +36,7 @@ __device__ __forceinline__ void dual_at(const PdArgs& a, const Dims& d, int i, i
     if (!a.aniso) {
         const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
         if (den > 1.0f) {
-            const float sq = 1.0f / sqrtf(den);
+            const float sq = rsqrtf(den);  // within 2 ulp of 1/sqrtf
             p1 *= sq;
             p2 *= sq;
             p3 *= sq;

@@ -38,9 +38,10 @@ __device__ __forceinline__ void tgv_dual_tile(const TgvArgs& a, const Dims& d, i
         // ProjP (TGV_core.c:370-387)
         const float gp = (THREE ? sqrtf(p1 * p1 + p2 * p2 + p3 * p3) : sqrtf(p1 * p1 + p2 * p2)) / a.alpha1;
         if (gp > 1.0f) {
-            p1 /= gp;
-            p2 /= gp;
-            p3 /= gp;
+            const float ig = __frcp_rn(gp);  // one reciprocal instead of three divisions
+            p1 *= ig;
+            p2 *= ig;
+            p3 *= ig;
         }
         a.p[0][v] = p1;
         a.p[1][v] = p2;
@@ -60,7 +61,8 @@ __device__ __forceinline__ void tgv_dual_tile(const TgvArgs& a, const Dims& d, i
             float g = sqrtf(Q1 * Q1 + Q2 * Q2 + Q3 * Q3 + 2.0f * Q4 * Q4 + 2.0f * Q5 * Q5 + 2.0f * Q6 * Q6);
             g = g / a.alpha0;
             if (g > 1.0f) {
-                Q1 /= g; Q2 /= g; Q3 /= g; Q4 /= g; Q5 /= g; Q6 /= g;
+                const float ig = __frcp_rn(g);
+                Q1 *= ig; Q2 *= ig; Q3 *= ig; Q4 *= ig; Q5 *= ig; Q6 *= ig;
             }
             a.q[0][v] = Q1; a.q[1][v] = Q2; a.q[2][v] = Q3;
             a.q[3][v] = Q4; a.q[4][v] = Q5; a.q[5][v] = Q6;
@@ -73,7 +75,10 @@ __device__ __forceinline__ void tgv_dual_tile(const TgvArgs& a, const Dims& d, i
             float Q3 = a.q[2][v] + a.sigma * (0.5f * (q11 + q22));
             float g = sqrtf(Q1 * Q1 + Q2 * Q2 + 2.0f * Q3 * Q3);
             g = g / a.alpha0;
-            if (g > 1.0f) { Q1 /= g; Q2 /= g; Q3 /= g; }
+            if (g > 1.0f) {
+                const float ig = __frcp_rn(g);
+                Q1 *= ig; Q2 *= ig; Q3 *= ig;
+            }
             a.q[0][v] = Q1; a.q[1][v] = Q2; a.q[2][v] = Q3;
         }
     }
@@ -107,7 +112,7 @@ __device__ __forceinline__ void tgv_primal_tile(const TgvArgs& a, const Dims& d,
             float dv = bwd(a.p[0], v, 1, i, d.nx) + bwd(a.p[1], v, d.nx, j, d.ny);
             if (THREE) dv = dv + bwd(a.p[2], v, d.sxy, k, d.nz);
             const float uo = a.u[v];
-            const float un = (a.lambda * (uo + a.tau * dv) + a.tau * ldg(a.u0, v)) / (a.lambda + a.tau);
+            const float un = (a.lambda * (uo + a.tau * dv) + a.tau * ldg(a.u0, v)) * a.inv_lt;
             const float ue = 2.0f * un - uo;
             a.u[v] = ue;
             if (a.check) {
@@ -225,6 +230,7 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     a.alpha0 = alpha0;
     a.tau = (float)pow((double)L2, -0.5);  // TGV_core.c:54-55
     a.sigma = a.tau;
+    a.inv_lt = 1.0f / (a.lambda + a.tau);
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;

@@ -12,6 +12,7 @@ struct TgvArgs {
     float* q[6];
     float* v[3];
     float lambda, alpha1, alpha0, tau, sigma;
+    float inv_lt;  // 1 / (lambda + tau)
     int check;
 };
 
