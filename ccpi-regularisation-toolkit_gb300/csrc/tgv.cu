@@ -84,11 +84,6 @@ __device__ __forceinline__ void tgv_dual_tile(const TgvArgs& a, const Dims& d, i
     }
 }
 
-template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_dual(TgvArgs a, Dims d, int kz, const StopCtl* ctl) {
-    if (ctl->stop) return;
-    tgv_dual_tile<THREE>(a, d, kz, blockIdx.x, blockIdx.y, blockIdx.z);
-}
 
 // backward difference with the reference's three-case boundary (TGV_core.c:286-292)
 __device__ __forceinline__ float bwd(const float* X, long long v, long long stride, int i, int n) {
@@ -145,18 +140,133 @@ __device__ __forceinline__ void tgv_primal_tile(const TgvArgs& a, const Dims& d,
     }
 }
 
+
+// single-volume kernels: the kernel parameter struct is read directly (a
+// reference to it would copy the whole struct into registers)
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_primal(TgvArgs a, Dims d, int kz, const StopCtl* ctl,
+__global__ void __launch_bounds__(256) k_tgv_dual(TgvArgs a, Dims d, int kz, const StopCtl* ctl) {
+    if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
+    if (i >= d.nx || j >= d.ny) return;
+    const bool xe = (i == d.nx - 1), ye = (j == d.ny - 1);
+    for (int kk = 0; kk < kz; kk++) {
+        const int k = k0 + kk;
+        if (k >= d.nz) break;
+        const bool ze = (k == d.nz - 1);
+        const long long v = vid(d, i, j, k);
+        const long long vx = v + 1, vy = v + d.nx, vz = v + d.sxy;
+        const float u = a.u[v];
+        const float v1 = a.v[0][v], v2 = a.v[1][v], v3 = THREE ? a.v[2][v] : 0.0f;
+        // DualP (TGV_core.c:351-368)
+        float p1 = a.p[0][v] + (xe ? a.sigma * (-v1) : a.sigma * ((a.u[vx] - u) - v1));
+        float p2 = a.p[1][v] + (ye ? a.sigma * (-v2) : a.sigma * ((a.u[vy] - u) - v2));
+        float p3 = 0.0f;
+        if (THREE) p3 = a.p[2][v] + (ze ? a.sigma * (-v3) : a.sigma * ((a.u[vz] - u) - v3));
+        // ProjP (TGV_core.c:370-387)
+        const float gp = (THREE ? sqrtf(p1 * p1 + p2 * p2 + p3 * p3) : sqrtf(p1 * p1 + p2 * p2)) / a.alpha1;
+        if (gp > 1.0f) {
+            const float ig = __frcp_rn(gp);  // one reciprocal instead of three divisions
+            p1 *= ig;
+            p2 *= ig;
+            p3 *= ig;
+        }
+        a.p[0][v] = p1;
+        a.p[1][v] = p2;
+        if (THREE) a.p[2][v] = p3;
+        // DualQ + ProjQ (TGV_core.c:389-446 / 234-275)
+        if (THREE) {
+            float q1 = 0, q11 = 0, q33 = 0, q2 = 0, q22 = 0, q55 = 0, q3 = 0, q44 = 0, q66 = 0;
+            if (!xe) { q1 = a.v[0][vx] - v1; q11 = a.v[1][vx] - v2; q33 = a.v[2][vx] - v3; }
+            if (!ye) { q2 = a.v[1][vy] - v2; q22 = a.v[0][vy] - v1; q55 = a.v[2][vy] - v3; }
+            if (!ze) { q3 = a.v[2][vz] - v3; q44 = a.v[0][vz] - v1; q66 = a.v[1][vz] - v2; }
+            float Q1 = a.q[0][v] + a.sigma * q1;
+            float Q2 = a.q[1][v] + a.sigma * q2;
+            float Q3 = a.q[2][v] + a.sigma * q3;
+            float Q4 = a.q[3][v] + a.sigma * (0.5f * (q11 + q22));
+            float Q5 = a.q[4][v] + a.sigma * (0.5f * (q33 + q44));
+            float Q6 = a.q[5][v] + a.sigma * (0.5f * (q55 + q66));
+            float g = sqrtf(Q1 * Q1 + Q2 * Q2 + Q3 * Q3 + 2.0f * Q4 * Q4 + 2.0f * Q5 * Q5 + 2.0f * Q6 * Q6);
+            g = g / a.alpha0;
+            if (g > 1.0f) {
+                const float ig = __frcp_rn(g);
+                Q1 *= ig; Q2 *= ig; Q3 *= ig; Q4 *= ig; Q5 *= ig; Q6 *= ig;
+            }
+            a.q[0][v] = Q1; a.q[1][v] = Q2; a.q[2][v] = Q3;
+            a.q[3][v] = Q4; a.q[4][v] = Q5; a.q[5][v] = Q6;
+        } else {
+            float q1 = 0, q11 = 0, q2 = 0, q22 = 0;
+            if (!xe) { q1 = a.v[0][vx] - v1; q11 = a.v[1][vx] - v2; }
+            if (!ye) { q2 = a.v[1][vy] - v2; q22 = a.v[0][vy] - v1; }
+            float Q1 = a.q[0][v] + a.sigma * q1;
+            float Q2 = a.q[1][v] + a.sigma * q2;
+            float Q3 = a.q[2][v] + a.sigma * (0.5f * (q11 + q22));
+            float g = sqrtf(Q1 * Q1 + Q2 * Q2 + 2.0f * Q3 * Q3);
+            g = g / a.alpha0;
+            if (g > 1.0f) {
+                const float ig = __frcp_rn(g);
+                Q1 *= ig; Q2 *= ig; Q3 *= ig;
+            }
+            a.q[0][v] = Q1; a.q[1][v] = Q2; a.q[2][v] = Q3;
+        }
+    }
+}
+
+template <bool THREE>
+__global__ void __launch_bounds__(256, 6) k_tgv_primal(TgvArgs a, Dims d, int kz, const StopCtl* ctl,
                                                     double2* partials) {
     if (ctl->stop) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k0 = blockIdx.z * kz;
     float pa = 0.0f, pb = 0.0f;
-    tgv_primal_tile<THREE>(a, d, kz, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
+    if (i < d.nx && j < d.ny) {
+        for (int kk = 0; kk < kz; kk++) {
+            const int k = k0 + kk;
+            if (k >= d.nz) break;
+            const long long v = vid(d, i, j, k);
+            // DivProjP + newU (TGV_core.c:448-472, 548-554)
+            float dv = bwd(a.p[0], v, 1, i, d.nx) + bwd(a.p[1], v, d.nx, j, d.ny);
+            if (THREE) dv = dv + bwd(a.p[2], v, d.sxy, k, d.nz);
+            const float uo = a.u[v];
+            const float un = (a.lambda * (uo + a.tau * dv) + a.tau * ldg(a.u0, v)) * a.inv_lt;
+            const float ue = 2.0f * un - uo;
+            a.u[v] = ue;
+            if (a.check) {
+                const float df = ue - uo;
+                pa += df * df;
+                pb += ue * ue;
+            }
+            // UpdV + newV (TGV_core.c:474-533, 558-568)
+            if (THREE) {
+                const float q1 = bwd(a.q[0], v, 1, i, d.nx), q4x = bwd(a.q[3], v, 1, i, d.nx),
+                            q5x = bwd(a.q[4], v, 1, i, d.nx);
+                const float q2 = bwd(a.q[1], v, d.nx, j, d.ny), q4y = bwd(a.q[3], v, d.nx, j, d.ny),
+                            q6y = bwd(a.q[5], v, d.nx, j, d.ny);
+                const float q6z = bwd(a.q[5], v, d.sxy, k, d.nz), q5z = bwd(a.q[4], v, d.sxy, k, d.nz),
+                            q3 = bwd(a.q[2], v, d.sxy, k, d.nz);
+                const float d1 = q1 + q4y + q5z, d2 = q4x + q2 + q6z, d3 = q5x + q6y + q3;
+                const float v1 = a.v[0][v], v2 = a.v[1][v], v3 = a.v[2][v];
+                a.v[0][v] = 2.0f * (v1 + a.tau * (a.p[0][v] + d1)) - v1;
+                a.v[1][v] = 2.0f * (v2 + a.tau * (a.p[1][v] + d2)) - v2;
+                a.v[2][v] = 2.0f * (v3 + a.tau * (a.p[2][v] + d3)) - v3;
+            } else {
+                const float q1 = bwd(a.q[0], v, 1, i, d.nx), q3x = bwd(a.q[2], v, 1, i, d.nx);
+                const float q2 = bwd(a.q[1], v, d.nx, j, d.ny), q3y = bwd(a.q[2], v, d.nx, j, d.ny);
+                const float d1 = q1 + q3y, d2 = q3x + q2;
+                const float v1 = a.v[0][v], v2 = a.v[1][v];
+                a.v[0][v] = 2.0f * (v1 + a.tau * (a.p[0][v] + d1)) - v1;
+                a.v[1][v] = 2.0f * (v2 + a.tau * (a.p[1][v] + d2)) - v2;
+            }
+        }
+    }
     if (a.check) block_pair_partial<256>(pa, pb, partials, block_slot());
 }
 
 // batched: one flat grid over the tiles of every volume
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_dual_batch(const TgvBatchVol* __restrict__ vols,
+__global__ void __launch_bounds__(256, 4) k_tgv_dual_batch(const TgvBatchVol* __restrict__ vols,
                                                         const int* __restrict__ tile_vol) {
     const long long t = blockIdx.x;
     const TgvBatchVol& V = vols[tile_vol[t]];
@@ -168,7 +278,7 @@ __global__ void __launch_bounds__(256) k_tgv_dual_batch(const TgvBatchVol* __res
 }
 
 template <bool THREE>
-__global__ void __launch_bounds__(256) k_tgv_primal_batch(const TgvBatchVol* __restrict__ vols,
+__global__ void __launch_bounds__(256, 4) k_tgv_primal_batch(const TgvBatchVol* __restrict__ vols,
                                                           const int* __restrict__ tile_vol, int check) {
     const long long t = blockIdx.x;
     const TgvBatchVol& V = vols[tile_vol[t]];

@@ -7,7 +7,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _requests(n, seed):
+def _requests(n, seed, spacing=0.004):
     from ccpi.filters.serving import ProxRequest
 
     rng = np.random.default_rng(seed)
@@ -18,7 +18,7 @@ def _requests(n, seed):
         shape = (48, 64) if i % 3 == 0 else (16, 20, 24)
         vol = rng.random(shape).astype(np.float32)
         reqs.append(ProxRequest(i, alg, vol, prm, outer=int(rng.integers(2, 6)), inner=7,
-                                arrival=0.004 * i))
+                                arrival=spacing * i))
     return reqs
 
 
@@ -26,7 +26,7 @@ def test_result_same_alone_and_in_the_mix():
     import torch
     from ccpi.filters.serving import ProxServer, run_one
 
-    reqs = _requests(12, 1)
+    reqs = _requests(12, 1, spacing=0.0)  # a burst: four requests start together
     mixed = ProxServer(slots=4).serve(reqs)
     s = torch.cuda.Stream()
     for r, got in zip(reqs, mixed):
