@@ -4,7 +4,10 @@
 // Two kernels per iteration: the weighted Laplacian W of U (19-point stencil
 // in 3D), then U += tau (-lambda Lap(W) - (U - f)) in place (each voxel
 // reads W at its mirrored neighbours and U, f at itself only).
+#include "diff4th_tiled.cuh"
 #include "drivers.cuh"
+
+#include <stdlib.h>
 
 namespace cilreg {
 
@@ -110,13 +113,34 @@ int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters,
     const bool three = d.nz > 1;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    // CILREG_D4_KERNEL=simple selects the two per-voxel kernels (kept for A/B checks)
+    const char* ek = getenv("CILREG_D4_KERNEL");
+    const bool stream = !(ek && ek[0] == 's');
+    const D4Plan T = d4_stream_plan(d);
+    IterControl ctl(s, scratch, iters, epsil, stream ? T.nblocks : num_blocks(L));
     CILREG_TRY(ctl.status());
     float* W = scratch.floats(d.n);
     if (!W) return scratch.status();
     CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     const float sg2 = sigma * sigma;  // Diffus4th_order_core.c:51
     const float isg2 = 1.0f / sg2;    // den / sg2 formed as den * isg2 (within 1 ulp)
+    if (stream) {
+        // fused iteration, ping-pong between u_out and W's buffer
+        float* bufs[2] = {u_out, W};
+        int it = 0;
+        for (; it < iters; it++) {
+            const int check = ctl.is_check(it) ? 1 : 0;
+            CILREG_TRY(d4_stream_step(T, bufs[it & 1], bufs[(it + 1) & 1], f, lam, tau, isg2, d, ctl.ctl(), check,
+                                      ctl.partials(), s));
+            note_launch();
+            if (check) {
+                CILREG_TRY(ctl.after_check(it, T.nblocks));
+                if (ctl.host_should_stop()) break;
+            }
+        }
+        if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, bufs, u_out, d.n, s));
+        return ctl.finish(info);
+    }
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;

@@ -6,6 +6,9 @@
 // neighbours, so P never makes a second pass through HBM.  Traffic per
 // voxel-iteration: read Ue, P(3), f; write Ue, P(3) -> 36 B in 3D.
 #include "drivers.cuh"
+#include "pd_tiled.cuh"
+
+#include <stdlib.h>
 
 namespace cilreg {
 
@@ -110,7 +113,12 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    // CILREG_PD_KERNEL=simple selects the per-voxel kernel (kept for A/B checks)
+    const char* ek = getenv("CILREG_PD_KERNEL");
+    const bool stream = !(ek && ek[0] == 's');
+    const PdPlan T = pd_stream_plan(d);
+    const long long nparts = stream ? T.nblocks : num_blocks(L);
+    IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());
     float* ub[2];
     float* pb[2][3] = {};
@@ -150,14 +158,34 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
         a.nonneg = (nonneg == 1);
         a.aniso = (methodTV != 0);
         a.check = check;
-        if (three)
+        if (stream) {
+            PdStreamArgs b;
+            b.u = a.u;
+            b.un = a.un;
+            for (int c = 0; c < 3; c++) {
+                b.p[c] = a.p[c];
+                b.pn[c] = a.pn[c];
+            }
+            b.f = f;
+            b.ubrk = u_out;
+            b.sigma = sigma;
+            b.tau = tau;
+            b.lt = lt;
+            b.inv_onelt = (float)(1.0 / (1.0 + (double)lt));  // the reference divides by (1.0 + lt)
+            b.theta = 1.0f;
+            b.nonneg = a.nonneg;
+            b.aniso = a.aniso;
+            b.check = check;
+            CILREG_TRY(pd_stream_step(T, b, d, ctl.ctl(), ctl.partials(), s));
+        } else if (three) {
             k_pd_step<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
-        else
+        } else {
             k_pd_step<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+        }
         CILREG_CUDA(cudaGetLastError());
         note_launch();
         if (check) {
-            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            CILREG_TRY(ctl.after_check(it, nparts));
             if (ctl.host_should_stop()) break;
         }
     }

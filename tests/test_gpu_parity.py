@@ -232,3 +232,39 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         monkeypatch.delenv("CILREG_ROF_KERNEL")
         assert int(ia[0]) == int(ib[0])
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
+                         ids=str)
+def test_pd_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
+    """The 2.5D streaming PD kernel and the per-voxel kernel compute the same iteration."""
+    from ccpi.filters.regularisers import PD_TV
+
+    rng = np.random.default_rng(13 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = PD_TV(x, 0.05, 70, epsil, 8.0, method, nonneg, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_PD_KERNEL", "simple")
+        b = PD_TV(x, 0.05, 70, epsil, 8.0, method, nonneg, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_PD_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
+                         ids=str)
+def test_diff4th_streaming_kernel_equals_per_voxel_kernels(shape, monkeypatch):
+    """The 2.5D streaming Diff4th kernel and the two per-voxel kernels compute the same iteration."""
+    from ccpi.filters.regularisers import Diff4th
+
+    rng = np.random.default_rng(17 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil in (0.0, 1e-3):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = Diff4th(x, 0.8, 0.02, 60, 1e-4, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_D4_KERNEL", "simple")
+        b = Diff4th(x, 0.8, 0.02, 60, 1e-4, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_D4_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
