@@ -245,6 +245,8 @@ def suite(args):
         t = torch.from_numpy(noisy_phantom(shape, 30 if len(shape) == 3 else 10, 1 if len(shape) == 3 else 0)).cuda()
         n = t.numel()
         for name, fn in calls.items():
+            if args.regs and name not in args.regs.split(","):
+                continue
             i1, i2 = (10, 40) if len(shape) == 3 else (50, 450)
 
             def timed(iters):
@@ -425,6 +427,7 @@ def main():
     ap.add_argument("--serve", action="store_true",
                     help="Poisson stream (mean 200 req/s) of prox requests through the continuous-batching server")
     ap.add_argument("--requests", type=int, default=48, help="requests of the --serve stream")
+    ap.add_argument("--regs", default="", help="comma-separated regularisers of --suite (default: all)")
     ap.add_argument("--suite", action="store_true",
                     help="per-regulariser iteration time and roofline fraction (device data, fixed counts)")
     args = ap.parse_args()

@@ -229,8 +229,16 @@ TiledPlan fgp_tiled_plan(const Dims& d) {
     TiledPlan T;
     const char* e = getenv("CILREG_FGP_KERNEL");
     T.use = !(e && e[0] == 's');  // "simple" selects the per-voxel kernel of fgp.cu
-    T.zchunk = fgp_default_zchunk(d);
     T.block = dim3(BX, BY, 1);
+    if (d.nz > 1) {
+        // one volume: balance the CTAs over the SMs (the batched path packs
+        // many volumes and keeps fgp_default_zchunk)
+        static const int resident = resident_ctas(k_fgp_stream<true>, NT);
+        const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
+        T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
+    } else {
+        T.zchunk = 1;
+    }
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
     return T;

@@ -137,8 +137,14 @@ __global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int
 
 PdPlan pd_stream_plan(const Dims& d) {
     PdPlan T;
-    T.zchunk = (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1;
     T.block = dim3(BX, BY, 1);
+    if (d.nz > 1) {
+        static const int resident = resident_ctas(k_pd_stream<true>, NT);
+        const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
+        T.zchunk = wave_zchunk(tiles, d.nz, resident, 1, ZCHUNK);
+    } else {
+        T.zchunk = 1;
+    }
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
     return T;

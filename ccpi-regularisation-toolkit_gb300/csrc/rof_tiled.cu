@@ -2,23 +2,30 @@
 //
 // Reference arithmetic: ROF_TV_core.c:102-317.  Per voxel the update needs the
 // three normalised fluxes D1 (j axis), D2 (i axis), D3 (k axis) at the voxel
-// and at its mirrored lower neighbour on the same axis; each flux needs U on
-// the 7-point mirrored neighbourhood.
+// and at its mirrored lower neighbour on the same axis.  D1 needs U at the
+// voxel, its upper j neighbour and both i neighbours (minmod); D2 the mirror
+// image of that; so the update of a voxel reads U only within one voxel of it
+// in i and j, and the lower-neighbour fluxes D1(j-1), D2(i-1) need no U beyond
+// that either.
 //
-// A CTA of 32 x 16 threads holds an overlapping tile: thread (tx, ty) sits on
-// voxel (x0 - 2 + tx, y0 - 2 + ty); fluxes are formed on the inner 30 x 14
-// voxels and the update on the inner 28 x 12.  Walking a chunk of z planes,
-// step j of each thread:
-//   A. forms the fluxes of plane j-1 once per voxel (three minmods, three
-//      normalisations) from U of plane j-1 in shared memory (x/y
-//      neighbours) and its own registers U(j-2), U(j) (z neighbours);
-//      D1, D2 go to shared memory, D3 stays in a register;
-//   B. publishes U(j) (prefetched one step earlier) to shared memory;
-//   C. updates plane j-2: U += tau (lambda div D - (U - f)), with D3 of the
-//      lower z neighbour from its own registers (plane 1 when j-2 == 0,
-//      the mirror of ROF_TV_core.c:287).
-// One barrier per plane; mirrored boundaries are neighbour-index selections.
-// HBM traffic: read U and f, write U (12 B/voxel) plus the tile halo from L2.
+// A CTA of 32 x 16 threads holds an overlapping tile with a one-voxel halo:
+// thread (tx, ty) sits on voxel (x0 - 1 + tx, y0 - 1 + ty) and the inner
+// 30 x 14 voxels are updated.  Walking a chunk of z planes, step j of each
+// thread:
+//   A. forms the fluxes of plane j-1 (three minmods, three normalisations)
+//      from U of plane j-1 in shared memory (i/j neighbours) and its own
+//      registers U(j-2), U(j) (k neighbours); D1, D2 go to shared memory, all
+//      three stay in registers for the thread's own update;
+//   B. publishes U(j) (loaded two steps earlier) to shared memory;
+//   C. updates plane j-2: U += tau (lambda div D - (U - f)).
+// One barrier per plane.  The i/j mirrors are per-thread neighbour offsets
+// and the k mirror two selects on the plane index, so the steady loop has no
+// boundary branches; shared-memory ring slots are compile-time constants
+// (the loop is unrolled by two).  The z chunk length balances the CTAs over
+// the SMs (wave_zchunk).  HBM traffic: read U and f, write U
+// (12 B/voxel) plus the tile halo from L2.
+#include <type_traits>
+
 #include "rof_tiled.cuh"
 
 namespace cilreg {
@@ -26,149 +33,181 @@ namespace cilreg {
 namespace {
 
 constexpr int BX = 32, BY = 16;
-constexpr int OX = BX - 4, OY = BY - 4;  // updated voxels per tile
+constexpr int OX = BX - 2, OY = BY - 2;  // updated voxels per tile
 constexpr int NT = BX * BY;
 constexpr int ZCHUNK = 64;
 
-// 0.5 (sign a + sign b) min(|a|, |b|) of ROF_TV_core.c:132, as sign-case selects
-// (the same value: the smaller magnitude with the common sign, else 0)
-__device__ __forceinline__ float minmod(float a, float b) {
-    return (a > 0.f && b > 0.f) ? fminf(a, b) : ((a < 0.f && b < 0.f) ? fmaxf(a, b) : 0.f);
+// square of minmod(a, b) = 0.5 (sign a + sign b) min(|a|, |b|)
+// (ROF_TV_core.c:132): the median of a, b and 0 has the same magnitude
+__device__ __forceinline__ float minmod_sq(float a, float b) {
+    const float m = fmaxf(fminf(a, b), fminf(fmaxf(a, b), 0.f));
+    return m * m;
 }
 
 // dp / sqrt(s): one reciprocal square root instead of an IEEE square root and
 // division (within 2 ulp of the reference's quotient)
 __device__ __forceinline__ float normalise(float dp, float s) { return dp * rsqrtf(s); }
 
-template <bool THREE>
+template <int V>
+using Ic = std::integral_constant<int, V>;
+
+// IT: element-offset type (int when the volume has fewer than 2^31 voxels)
+template <bool THREE, bool CHECK, bool LARR, typename IT>
 __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                       const float* __restrict__ F, const float* __restrict__ lam_arr,
                                                       float lam, float tau, Dims d, int zc, const StopCtl* ctl,
-                                                      int check, double2* partials) {
-    __shared__ float sU[2][BY][BX];
-    __shared__ float sD1[2][BY][BX];
-    __shared__ float sD2[2][BY][BX];
+                                                      double2* partials) {
+    __shared__ float sU[2][BY * BX];
+    __shared__ float sD1[2][BY * BX];
+    __shared__ float sD2[2][BY * BX];
     if (ctl->stop) return;
+    const float EPS = 1.0e-8f;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int x = blockIdx.x * OX + tx - 2;
-    const int y = blockIdx.y * OY + ty - 2;
-    const int z0 = blockIdx.z * zc;
-    const int z1 = min(z0 + zc, nz);
+    const int x = blockIdx.x * OX + tx - 1;
+    const int y = blockIdx.y * OY + ty - 1;
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
-    const bool d_pt = in_xy && tx >= 1 && tx <= BX - 2 && ty >= 1 && ty <= BY - 2;  // fluxes formed here
-    const bool o_pt = in_xy && tx >= 2 && tx <= BX - 3 && ty >= 2 && ty <= BY - 3;  // update written here
-    // mirrored neighbour columns/rows inside the tile (an axis of length 1 maps to itself)
-    const int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
-    const int xl = (nx == 1) ? tx : ((x - 1 < 0) ? tx + 1 : tx - 1);
-    const int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
-    const int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
-    const long long col = in_xy ? ((long long)y * nx + x) : 0;
-    auto load_u = [&](int k) -> float {
-        return (in_xy && k >= 0 && k < nz) ? __ldg(U + (long long)k * d.sxy + col) : 0.f;
-    };
-
-    // f (and lambda) of plane k, needed only where the update is written
-    auto load_f = [&](int k, float& fv, float& lv) {
-        fv = 0.f;
-        lv = lam;
-        if (o_pt && k >= z0 && k < z1) {
-            const long long v = (long long)k * d.sxy + col;
-            fv = __ldg(F + v);
-            if (lam_arr) lv = __ldg(lam_arr + v);
-        }
-    };
-
-    // register pipeline: U is loaded two planes before it is published, f two
-    // planes before its update, so about two planes of loads are in flight
-    float um2 = load_u(z0 - 2), um1 = load_u(z0 - 1);  // U(j-2), U(j-1) at step j = z0
-    float uj = load_u(z0);                             // U(j)
-    float uq = load_u(z0 + 1);                         // U(j+1)
-    float fa, la, fb, lb;                              // f, lambda of planes j-2 and j-1
-    load_f(z0 - 2, fa, la);
-    load_f(z0 - 1, fb, lb);
-    float d3a = 0.f, d3b = 0.f, d3c = 0.f;             // D3 of planes j-1, j-2, j-3
+    const bool o_pt = in_xy && tx >= 1 && tx <= BX - 2 && ty >= 1 && ty <= BY - 2;
+    // neighbour columns / rows in the tile: mirrored at the volume edge (an axis
+    // of length 1 maps to itself), clamped to the tile elsewhere (a clamped
+    // neighbour only feeds fluxes that no update reads)
+    int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
+    int xl = (nx == 1) ? tx : ((x - 1 < 0) ? tx + 1 : tx - 1);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    xh = min(max(xh, 0), BX - 1);
+    xl = min(max(xl, 0), BX - 1);
+    yh = min(max(yh, 0), BY - 1);
+    yl = min(max(yl, 0), BY - 1);
+    const int oc = ty * BX + tx;
+    const int oxh = ty * BX + xh, oxl = ty * BX + xl, oyh = yh * BX + tx, oyl = yl * BX + tx;
+    // halo threads outside the volume load the nearest voxel inside it (their
+    // fluxes are never read), so loads need no predicate
+    const IT col = (IT)min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
     float pa = 0.f, pb = 0.f;
-    sU[(z0 - 1) & 1][ty][tx] = um1;
-    __syncthreads();
 
-    for (int j = z0; j <= z1 + 1; ++j) {
-        const float un2 = (j + 2 <= z1) ? load_u(j + 2) : 0.f;  // prefetch U(j+2)
-        float fn, ln;
-        load_f(j, fn, ln);                                      // prefetch f(j)
-        const int kf = j - 2;                                   // plane updated in step C
-        const float fk = fa, lk = la;
-        // A. fluxes of plane m = j-1
-        const int m = j - 1;
-        d3c = d3b;
-        d3b = d3a;
-        d3a = 0.f;
-        if (m >= z0 - 1 && m >= 0 && m < nz && m <= z1 - 1) {
-            const int sm = m & 1;
-            if (d_pt) {
-                const float c = sU[sm][ty][tx];
-                const float xp = sU[sm][ty][xh] - c, xm = c - sU[sm][ty][xl];
-                const float yp = sU[sm][yh][tx] - c, ym = c - sU[sm][yl][tx];
-                const float mx = minmod(xp, xm), my = minmod(yp, ym);
-                float d1, d2;
-                if (THREE) {
-                    const float zlo = (m == 0) ? uj : um2;          // mirrored lower plane
-                    const float zhi = (m == nz - 1) ? um2 : uj;     // mirrored upper plane
-                    const float zp = zhi - c, zm = c - zlo;
-                    const float mz = minmod(zp, zm);
-                    d1 = normalise(yp, yp * yp + mx * mx + mz * mz + 1.0e-8f);
-                    d2 = normalise(xp, xp * xp + my * my + mz * mz + 1.0e-8f);
-                    d3a = normalise(zp, zp * zp + my * my + mx * mx + 1.0e-8f);
-                } else {
-                    d1 = normalise(yp, yp * yp + mx * mx + 1.0e-8f);
-                    d2 = normalise(xp, xp * xp + my * my + 1.0e-8f);
-                }
-                sD1[sm][ty][tx] = d1;
-                sD2[sm][ty][tx] = d2;
-            }
-        }
-        // B. publish U(j)
-        sU[j & 1][ty][tx] = uj;
-        // C. update plane kf = j-2 (fluxes of kf were published in the previous step)
-        if (o_pt && kf >= z0 && kf < z1) {
-            const int sk = kf & 1;
-            const float dv1 = sD1[sk][ty][tx] - sD1[sk][yl][tx];
-            const float dv2 = sD2[sk][ty][tx] - sD2[sk][ty][xl];
-            float div;
-            if (THREE) {
-                const float d3lo = (kf == 0) ? d3a : d3c;  // D3 of the mirrored lower plane
-                div = dv1 + dv2 + (d3b - d3lo);
-            } else {
-                div = dv1 + dv2;
-            }
-            const float u = um2;
-            const float un = u + tau * (lk * div - (u - fk));
-            Un[(long long)kf * d.sxy + col] = un;
-            if (check) {
-                const float df = un - u;
-                pa += df * df;
-                pb += un * un;
-            }
-        }
+    if constexpr (!THREE) {
+        // one plane: publish U, form D1/D2, update
+        const float u = __ldg(U + col);
+        const float fv = o_pt ? __ldg(F + col) : 0.f;
+        const float lv = (LARR && o_pt) ? __ldg(lam_arr + col) : lam;
+        sU[0][oc] = u;
         __syncthreads();
-        um2 = um1;
-        um1 = uj;
-        uj = uq;
-        uq = un2;
-        fa = fb;
-        la = lb;
-        fb = fn;
-        lb = ln;
+        const float xp = sU[0][oxh] - u, xm = u - sU[0][oxl];
+        const float yp = sU[0][oyh] - u, ym = u - sU[0][oyl];
+        const float mx2 = minmod_sq(xp, xm), my2 = minmod_sq(yp, ym);
+        const float d1 = normalise(yp, yp * yp + mx2 + EPS);
+        const float d2 = normalise(xp, xp * xp + my2 + EPS);
+        sD1[0][oc] = d1;
+        sD2[0][oc] = d2;
+        __syncthreads();
+        if (o_pt) {
+            const float div = (d1 - sD1[0][oyl]) + (d2 - sD2[0][oxl]);
+            const float un = u + tau * (lv * div - (u - fv));
+            Un[col] = un;
+            if (CHECK) {
+                const float df = un - u;
+                pa = df * df;
+                pb = un * un;
+            }
+        }
+    } else {
+        const int z0 = blockIdx.z * zc;
+        const int z1 = min(z0 + zc, nz);
+        const IT sxy = (IT)d.sxy;
+        // element offset of plane k (clamped into the volume: planes outside it
+        // are loaded only into pipeline slots that are never used unmirrored)
+        auto at = [&](int k) -> IT { return (IT)min(max(k, 0), nz - 1) * sxy + col; };
+        auto ld_u = [&](int k) -> float { return __ldg(U + at(k)); };
+        auto ld_f = [&](int k, float& fv, float& lv) {
+            const IT o = at(k);
+            fv = o_pt ? __ldg(F + o) : 0.f;
+            lv = (LARR && o_pt) ? __ldg(lam_arr + o) : lam;
+        };
+        // registers entering step j: U(j-2), U(j-1), U(j), U(j+1); f and lambda of
+        // planes j-2, j-1; own fluxes of plane j-2 and D3 of plane j-3
+        float ua = ld_u(z0 - 2), ub = ld_u(z0 - 1), uc = ld_u(z0), ud = ld_u(z0 + 1);
+        float fa = 0.f, la = lam, fb = 0.f, lb = lam;
+        float d1o = 0.f, d2o = 0.f, d3o = 0.f, d3oo = 0.f;
+        sU[1][oc] = ub;  // ring slot of plane p: (p - z0) & 1
+        __syncthreads();
+
+        auto step = [&](auto par, auto full, int j) {
+            constexpr int P = decltype(par)::value;    // ring slot of plane j
+            constexpr bool FULL = decltype(full)::value;  // plane j-2 is updated
+            const float ue = ld_u(j + 2);
+            float fe, le;
+            ld_f(j, fe, le);  // f, lambda of plane j (its update is two steps on)
+            // A. fluxes of plane m = j-1 (ROF_TV_core.c:102-266); k neighbours
+            // mirrored at the first and last plane (ROF_TV_core.c:117-118)
+            const int m = j - 1;
+            const float zlo = (m == 0) ? uc : ua;
+            const float zhi = (m == nz - 1) ? ua : uc;
+            const float xp = sU[1 - P][oxh] - ub, xm = ub - sU[1 - P][oxl];
+            const float yp = sU[1 - P][oyh] - ub, ym = ub - sU[1 - P][oyl];
+            const float zp = zhi - ub, zm = ub - zlo;
+            const float mx2 = minmod_sq(xp, xm), my2 = minmod_sq(yp, ym), mz2 = minmod_sq(zp, zm);
+            const float n1 = normalise(yp, yp * yp + mx2 + mz2 + EPS);
+            const float n2 = normalise(xp, xp * xp + my2 + mz2 + EPS);
+            const float n3 = normalise(zp, zp * zp + my2 + mx2 + EPS);
+            sD1[1 - P][oc] = n1;
+            sD2[1 - P][oc] = n2;
+            // B. publish U(j)
+            sU[P][oc] = uc;
+            // C. update plane j-2 (ROF_TV_core.c:269-297); its fluxes were
+            // published in the previous step, the lower k flux is D3 of plane
+            // j-3, mirrored to plane 1 at the first plane
+            if (FULL) {
+                const int kf = j - 2;
+                const float d3lo = (kf == 0) ? n3 : d3oo;
+                const float div = (d1o - sD1[P][oyl]) + (d2o - sD2[P][oxl]) + (d3o - d3lo);
+                const float un = ua + tau * (la * div - (ua - fa));
+                if (o_pt) Un[(IT)kf * sxy + col] = un;
+                if (CHECK && o_pt) {
+                    const float df = un - ua;
+                    pa += df * df;
+                    pb += un * un;
+                }
+            }
+            __syncthreads();
+            ua = ub;
+            ub = uc;
+            uc = ud;
+            ud = ue;
+            fa = fb;
+            la = lb;
+            fb = fe;
+            lb = le;
+            d3oo = d3o;
+            d1o = n1;
+            d2o = n2;
+            d3o = n3;
+        };
+        step(Ic<0>{}, std::false_type{}, z0);
+        step(Ic<1>{}, std::false_type{}, z0 + 1);
+        int j = z0 + 2;
+        for (; j + 1 <= z1 + 1; j += 2) {
+            step(Ic<0>{}, std::true_type{}, j);
+            step(Ic<1>{}, std::true_type{}, j + 1);
+        }
+        if (j <= z1 + 1) step(Ic<0>{}, std::true_type{}, j);
     }
-    if (check) block_pair_partial<NT>(pa, pb, partials, block_slot());
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
 }  // namespace
 
 RofPlan rof_tiled_plan(const Dims& d) {
     RofPlan T;
-    T.zchunk = (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1;
     T.block = dim3(BX, BY, 1);
+    const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
+    if (d.nz > 1) {
+        // CTAs per SM of the 3D kernel (every variant has the same register cap)
+        static const int resident = resident_ctas(k_rof_stream<true, false, false, int>, NT);
+        T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
+    } else {
+        T.zchunk = 1;
+    }
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
     return T;
@@ -176,12 +215,20 @@ RofPlan rof_tiled_plan(const Dims& d) {
 
 int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,
                    float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
-    if (d.nz > 1)
-        k_rof_stream<true><<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, check,
-                                                      partials);
-    else
-        k_rof_stream<false><<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, check,
-                                                       partials);
+    const bool three = d.nz > 1, larr = lam_arr != nullptr;
+    decltype(&k_rof_stream<true, true, true, int>) kern;
+    if (d.n < (1LL << 31)) {
+        kern = three ? (check ? (larr ? k_rof_stream<true, true, true, int> : k_rof_stream<true, true, false, int>)
+                              : (larr ? k_rof_stream<true, false, true, int> : k_rof_stream<true, false, false, int>))
+                     : (check ? (larr ? k_rof_stream<false, true, true, int> : k_rof_stream<false, true, false, int>)
+                              : (larr ? k_rof_stream<false, false, true, int> : k_rof_stream<false, false, false, int>));
+    } else {
+        kern = three ? (check ? (larr ? k_rof_stream<true, true, true, long long> : k_rof_stream<true, true, false, long long>)
+                              : (larr ? k_rof_stream<true, false, true, long long> : k_rof_stream<true, false, false, long long>))
+                     : (check ? (larr ? k_rof_stream<false, true, true, long long> : k_rof_stream<false, true, false, long long>)
+                              : (larr ? k_rof_stream<false, false, true, long long> : k_rof_stream<false, false, false, long long>));
+    }
+    kern<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

@@ -2,6 +2,7 @@
 #include "runtime.cuh"
 
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -70,6 +71,41 @@ cudaStream_t thread_stream(int dev) {
         if (cudaStreamCreateWithFlags(&ts.s[dev], cudaStreamNonBlocking) != cudaSuccess) ts.s[dev] = 0;
     }
     return ts.s[dev];
+}
+
+int sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+        cache[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+int wave_zchunk(long long tiles_xy, int nz, int resident, int extra, int max_chunk) {
+    if (nz <= 1) return 1;
+    if (max_chunk > nz) max_chunk = nz;
+    if (const char* e = getenv("CILREG_STREAM_ZCHUNK")) {
+        const int v = atoi(e);
+        if (v > 0) return v < nz ? v : nz;
+    }
+    const long long slots = (long long)sm_count() * (resident > 0 ? resident : 1);
+    int best = max_chunk;
+    double best_cost = -1.0;
+    for (int zc = max_chunk; zc >= 8 || zc == max_chunk; zc--) {
+        const long long blocks = tiles_xy * ((nz + zc - 1) / zc);
+        const long long rounds = (blocks + slots - 1) / slots;
+        const double cost = (double)rounds * (double)(zc + extra);
+        if (best_cost < 0 || cost < best_cost * 0.995) {  // prefer longer chunks on ties
+            best_cost = cost;
+            best = zc;
+        }
+        if (zc <= 1) break;
+    }
+    return best;
 }
 
 // ---------------------------------------------------------------------------

@@ -48,6 +48,23 @@ int use_device(int dev);
 // a non-blocking stream owned by the calling host thread for device `dev`
 cudaStream_t thread_stream(int dev);
 
+// number of SMs of the current device (cached per device)
+int sm_count();
+
+// z-chunk length for a 2.5D streaming kernel: `tiles_xy` CTAs per z chunk,
+// `resident` CTAs per SM, `extra` pipeline steps per chunk besides its planes.
+// Minimises (rounds of CTAs over the SMs) x (steps per CTA), up to `max_chunk`.
+int wave_zchunk(long long tiles_xy, int nz, int resident, int extra, int max_chunk);
+
+// CTAs of `kernel` resident per SM at `threads` threads and no dynamic shared
+// memory (at least 1)
+template <class K>
+int resident_ctas(K kernel, int threads) {
+    int r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kernel, threads, 0) != cudaSuccess || r <= 0) r = 1;
+    return r;
+}
+
 // stream-ordered scratch buffers freed when the object is destroyed
 class Scratch {
 public:

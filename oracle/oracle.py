@@ -124,11 +124,18 @@ def _lib(use_ref):
 
 
 def rof_tv(x, lam, iters, tau, epsil, use_ref=False):
+    """`lam` is a scalar or a float32 array of x's shape (per-voxel lambda,
+    ROF_TV_core.c:280 `lambda_is_arr`)."""
     lib, is_port = _lib(use_ref)
     a, out, info = _prep(x)
-    lam_c = ctypes.c_float(lam)
     fn = lib.port_TV_ROF if is_port else lib.TV_ROF_CPU_main
-    fn(_ptr(a), _ptr(out), _ptr(info), ctypes.byref(lam_c), 0, iters, tau, epsil, *_dims(a))
+    if np.ndim(lam) == 0:
+        lam_c = ctypes.c_float(lam)
+        fn(_ptr(a), _ptr(out), _ptr(info), ctypes.byref(lam_c), 0, iters, tau, epsil, *_dims(a))
+    else:
+        lam_a = np.ascontiguousarray(lam, dtype=np.float32)
+        assert lam_a.shape == a.shape
+        fn(_ptr(a), _ptr(out), _ptr(info), _ptr(lam_a), 1, iters, tau, epsil, *_dims(a))
     return out, info
 
 

@@ -216,8 +216,8 @@ def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
-@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
-                         ids=str)
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
+                                   (130, 33, 35), (151, 12, 31)], ids=str)
 def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
     """The 2.5D streaming ROF kernel and the per-voxel kernel compute the same iteration."""
     from ccpi.filters.regularisers import ROF_TV
@@ -232,6 +232,26 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         monkeypatch.delenv("CILREG_ROF_KERNEL")
         assert int(ia[0]) == int(ib[0])
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(48, 61), (10, 16, 22), (70, 33, 35)], ids=str)
+def test_rof_per_voxel_lambda_matches_oracle(shape, monkeypatch):
+    """ROF with a per-voxel lambda map (ROF_TV_core.c:280 lambda_is_arr) through the
+    C-OMP entry point, against the oracle, on both GPU kernels."""
+    from ccpi.filters.TV import TV_ROF_CPU
+
+    rng = np.random.default_rng(29 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    lam = (0.005 + 0.04 * rng.random(shape)).astype(np.float32)
+    ref, iref = O.rof_tv(x, lam, 150, 0.002, 0.0)
+    for kernel in ("stream", "simple"):
+        if kernel == "simple":
+            monkeypatch.setenv("CILREG_ROF_KERNEL", "simple")
+        info = np.zeros(2, np.float32)
+        got = TV_ROF_CPU(x, lam, 150, 0.002, 0.0, infovector=info)
+        monkeypatch.delenv("CILREG_ROF_KERNEL", raising=False)
+        assert int(info[0]) == int(iref[0])
+        assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-5)
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
