@@ -6,37 +6,15 @@
 // result depends on the thread count).  Here every sweep reads the previous
 // iterate only (ping-pong buffers): deterministic, and equal to the
 // reference run with one thread up to the update order.  One kernel per
-// iteration; 12 B of HBM traffic per voxel-iteration.
+// iteration: the 2.5D streaming kernel of ndf_tiled.cu (12 B of HBM traffic
+// per voxel-iteration), or the per-voxel kernel below for CILREG_NDF_KERNEL=
+// simple and volumes of 2^31 voxels or more.
 #include "drivers.cuh"
+#include "ndf_tiled.cuh"
 
 namespace cilreg {
 
 namespace {
-
-// edge-stopping function of one neighbour difference (Diffusion_core.c:315-404)
-// (e / sigma is formed as e * isg, isg = 1/sigma from the host: one multiply
-// instead of an IEEE division, within 1 ulp of the reference's quotient)
-template <int PEN>
-__device__ __forceinline__ float flux(float e, float sg, float isg) {
-    if (PEN == 0) return e;  // linear diffusion (sigma == 0)
-    if (PEN == 1) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
-    if (PEN == 2) {
-        const float r = e * isg;
-        return e * __frcp_rn(1.0f + r * r);
-    }
-    if (PEN == 3) {
-        if (fabsf(e) <= sg) {
-            const float r = e * isg;
-            const float w = 1.0f - r * r;
-            return e * (w * w);
-        }
-        return 0.0f;
-    }
-    if (PEN == 4) return (fabsf(e) > sg) ? 0.0f : e;
-    // PEN == 5
-    if (fabsf(e) <= 2.0f * sg) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
-    return 0.0f;
-}
 
 template <bool THREE, int PEN>
 __global__ void __launch_bounds__(256) k_ndf_step(const float* __restrict__ U, float* __restrict__ Un,
@@ -110,7 +88,9 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     const bool three = d.nz > 1;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    const NdfPlan T = ndf_stream_plan(d);
+    const long long nparts = T.use ? T.nblocks : num_blocks(L);
+    IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());
     float* alt = scratch.floats(d.n);
     if (!alt) return scratch.status();
@@ -119,7 +99,10 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
-        if (three)
+        if (T.use)
+            CILREG_TRY(ndf_stream_step(T, pen, bufs[it & 1], bufs[(it + 1) & 1], f, lam, sg, isg, tau, d, ctl.ctl(),
+                                       check, ctl.partials(), s));
+        else if (three)
             launch_ndf<true>(pen, L, s, bufs[it & 1], bufs[(it + 1) & 1], f, lam, sg, isg, tau, d, ctl.ctl(), check,
                              ctl.partials());
         else
@@ -128,7 +111,7 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
         CILREG_CUDA(cudaGetLastError());
         note_launch();
         if (check) {
-            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            CILREG_TRY(ctl.after_check(it, nparts));
             if (ctl.host_should_stop()) break;
         }
     }

@@ -1,0 +1,51 @@
+// Non-linear diffusion: the edge-stopping function shared by the per-voxel
+// kernel (ndf.cu) and the 2.5D streaming kernel (ndf_tiled.cu), and the
+// streaming kernel's entry points.
+#pragma once
+
+#include "runtime.cuh"
+
+namespace cilreg {
+
+// edge-stopping function of one neighbour difference (Diffusion_core.c:315-404)
+// (e / sigma is formed as e * isg, isg = 1/sigma from the host: one multiply
+// instead of an IEEE division, within 1 ulp of the reference's quotient)
+template <int PEN>
+__device__ __forceinline__ float flux(float e, float sg, float isg) {
+    if (PEN == 0) return e;  // linear diffusion (sigma == 0)
+    if (PEN == 1) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
+    if (PEN == 2) {
+        const float r = e * isg;
+        return e * __frcp_rn(1.0f + r * r);
+    }
+    if (PEN == 3) {
+        if (fabsf(e) <= sg) {
+            const float r = e * isg;
+            const float w = 1.0f - r * r;
+            return e * (w * w);
+        }
+        return 0.0f;
+    }
+    if (PEN == 4) return (fabsf(e) > sg) ? 0.0f : e;
+    // PEN == 5
+    if (fabsf(e) <= 2.0f * sg) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
+    return 0.0f;
+}
+
+// Every penalty is odd (flux(-e) == -flux(e) bit for bit: the sign enters
+// only through e itself or sgnf(e)), so the flux through a face can be formed
+// once and used with opposite signs by the two voxels that share it.
+
+struct NdfPlan {
+    dim3 grid, block;
+    long long nblocks = 0;
+    int zchunk = 0;
+    bool use = false;  // false: the per-voxel kernel of ndf.cu runs instead
+};
+
+NdfPlan ndf_stream_plan(const Dims& d);
+int ndf_stream_step(const NdfPlan& T, int pen, const float* cur, float* nxt, const float* f, float lam, float sg,
+                    float isg, float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials,
+                    cudaStream_t s);
+
+}  // namespace cilreg

@@ -3,10 +3,13 @@
 // Per outer iteration: two Jacobi sweeps of the (mu + 2*dim*lambda) system
 // (the reference's gauss_seidel*, which read U_prev only), then shrinkage of
 // grad U + B into D and the Bregman update of B.  Kernels:
-//   k_sb_sweep   U_out = sweep(U_in, D, B, f)        (x2, ping-pong)
+//   k_sb_sweep2  both sweeps in one streaming pass (sb_tiled.cu)
+//   k_sb_sweep   U_out = sweep(U_in, D, B, f), x2 (CILREG_SB_KERNEL=simple,
+//                and volumes of 2^31 voxels or more)
 //   k_sb_shrink  D, B updated in place from the new U (one voxel each)
 // The stopping check compares the two sweeps' results (SB_TV_core.c:123-134).
 #include "drivers.cuh"
+#include "sb_tiled.cuh"
 
 namespace cilreg {
 
@@ -128,7 +131,9 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    const SbPlan T = sb_sweep2_plan(d);
+    const long long nparts = T.use ? T.nblocks : num_blocks(L);
+    IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());
     float* u1 = scratch.floats(d.n);
     if (!u1) return scratch.status();
@@ -156,6 +161,38 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
     a.aniso = (methodTV == 1);
     a.f = f;
     int it = 0;
+    if (T.use) {
+        // fused sweeps (U ping-pongs between u_out and u1), then the shrinkage
+        // and Bregman update of D, B in place from U2
+        float* bufs[2] = {u_out, u1};
+        SbSweepArgs w;
+        for (int c = 0; c < 3; c++) {
+            w.dd[c] = a.dd[c];
+            w.bb[c] = a.bb[c];
+        }
+        w.f = f;
+        w.lambda = a.lambda;
+        w.mu = a.mu;
+        w.norm = a.norm;
+        a.check = 0;
+        for (; it < iters; it++) {
+            const int check = ctl.is_check(it) ? 1 : 0;
+            w.u = bufs[it & 1];
+            w.u2 = bufs[(it + 1) & 1];
+            CILREG_TRY(sb_sweep2_step(T, w, d, ctl.ctl(), check, ctl.partials(), s));
+            a.u = w.u2;
+            if (three) k_sb_shrink<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+            else k_sb_shrink<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+            CILREG_CUDA(cudaGetLastError());
+            note_launch(2);
+            if (check) {
+                CILREG_TRY(ctl.after_check(it, nparts));
+                if (ctl.host_should_stop()) break;
+            }
+        }
+        if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, bufs, u_out, d.n, s));
+        return ctl.finish(info);
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         a.check = 0;
@@ -176,7 +213,7 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
         CILREG_CUDA(cudaGetLastError());
         note_launch(3);
         if (check) {
-            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            CILREG_TRY(ctl.after_check(it, nparts));
             if (ctl.host_should_stop()) break;
         }
     }

@@ -234,6 +234,47 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
+                                   (130, 33, 35)], ids=str)
+@pytest.mark.parametrize("penalty", [0, 1, 2, 3, 4, 5])
+def test_ndf_streaming_kernel_equals_per_voxel_kernel(shape, penalty, monkeypatch):
+    """The 2.5D streaming NDF kernel (one flux per face, used with both signs) and
+    the per-voxel kernel (six fluxes per voxel) compute the same iteration."""
+    from ccpi.filters.regularisers import NDF
+
+    rng = np.random.default_rng(17 + sum(shape) + penalty)
+    x = rng.random(shape).astype(np.float32)
+    sigma = 0.0 if penalty == 0 else 0.08
+    pen = 1 if penalty == 0 else penalty
+    for epsil in (0.0, 1e-3):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = NDF(x, 0.03, sigma, 90, 0.01, pen, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_NDF_KERNEL", "simple")
+        b = NDF(x, 0.03, sigma, 90, 0.01, pen, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_NDF_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
+                                   (130, 33, 35)], ids=str)
+def test_sb_fused_sweeps_equal_per_sweep_kernels(shape, monkeypatch):
+    """The fused two-sweep SB kernel and the per-sweep kernels compute the same
+    outer iteration (and the same stopping iteration)."""
+    from ccpi.filters.regularisers import SB_TV
+
+    rng = np.random.default_rng(23 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, epsil in ((0, 1e-3), (1, 0.0)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = SB_TV(x, 0.05, 60, epsil, method, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_SB_KERNEL", "simple")
+        b = SB_TV(x, 0.05, 60, epsil, method, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_SB_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
 @pytest.mark.parametrize("shape", [(48, 61), (10, 16, 22), (70, 33, 35)], ids=str)
 def test_rof_per_voxel_lambda_matches_oracle(shape, monkeypatch):
     """ROF with a per-voxel lambda map (ROF_TV_core.c:280 lambda_is_arr) through the
