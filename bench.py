@@ -51,6 +51,20 @@ def _env_rank():
         os.environ.get("LOCAL_RANK", "0"))
 
 
+def reduce_over_ranks(pg, t_local, units_local, device):
+    """Whole-job figures of independent replicas: (slowest rank's time, sum of
+    all ranks' units).  `pg` is torch.distributed (or None for one process)."""
+    if pg is None:
+        return float(t_local), float(units_local)
+    import torch
+
+    tt = torch.tensor([float(t_local), float(units_local)], device=device, dtype=torch.float64)
+    t_max, units = tt[:1].clone(), tt[1:].clone()
+    pg.all_reduce(t_max, op=pg.ReduceOp.MAX)
+    pg.all_reduce(units, op=pg.ReduceOp.SUM)
+    return float(t_max[0]), float(units[0])
+
+
 def _phantom(size):
     from ccpi.supp.phantoms import noisy_phantom
 
@@ -503,14 +517,7 @@ def main():
     clock_info = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     t_local = ms / 1e3
-    t_max = t_local
-    total_vi = n * iters_run
-    if pg is not None:
-        tt = torch.tensor([t_local, float(total_vi)], device=dev, dtype=torch.float64)
-        t_all = tt.clone()
-        pg.all_reduce(t_all[:1], op=pg.ReduceOp.MAX)
-        pg.all_reduce(t_all[1:], op=pg.ReduceOp.SUM)
-        t_max, total_vi = float(t_all[0]), float(t_all[1])
+    t_max, total_vi = reduce_over_ranks(pg, t_local, n * iters_run, dev)
     value = total_vi / t_max
 
     # steady-state launch time of the FGP iteration kernel: difference of two
@@ -556,12 +563,8 @@ def main():
         e2e_vi += n * int(info[0])
     barrier()
     e2e_t = time.perf_counter() - t0
-    e2e_val = e2e_vi / e2e_t
-    if pg is not None:
-        tt = torch.tensor([e2e_t, float(e2e_vi)], device=dev, dtype=torch.float64)
-        pg.all_reduce(tt[:1], op=pg.ReduceOp.MAX)
-        pg.all_reduce(tt[1:], op=pg.ReduceOp.SUM)
-        e2e_val = float(tt[1]) / float(tt[0])
+    e2e_t_max, e2e_vi_all = reduce_over_ranks(pg, e2e_t, e2e_vi, dev)
+    e2e_val = e2e_vi_all / e2e_t_max
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
