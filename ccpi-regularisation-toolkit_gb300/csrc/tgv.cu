@@ -4,11 +4,13 @@
 //   k_tgv_dual    P += sigma (grad U - V), |P| <= alpha1;
 //                 Q += sigma sym-grad V,   |Q|_F <= alpha0   (reads U, V at +1)
 //   k_tgv_primal  U <- 2 prox(U + tau div P) - U;  V <- 2 (V + tau (P + div Q)) - V
-//                 (reads P, Q at -1)
+//                 (reads P, Q at -1); a single volume runs the 2.5D streaming
+//                 version of it (tgv_tiled.cu) unless CILREG_TGV_KERNEL=simple
 // 3D state: U, P(3), Q(6), V(3) plus U0.  The dual and primal halves of the
 // reference's ten sweeps (TGV_core.c:136-167) collapse into these two.
 #include "drivers.cuh"
 #include "tgv_batch.cuh"
+#include "tgv_tiled.cuh"
 
 namespace cilreg {
 
@@ -315,7 +317,9 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     const int np = three ? 3 : 2, nq = three ? 6 : 3;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    IterControl ctl(s, scratch, iters, epsil, num_blocks(L));
+    const TgvPlan T = tgv_primal_plan(d);
+    const long long nparts = T.use ? T.nblocks : num_blocks(L);
+    IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());
     TgvArgs a;
     for (int c = 0; c < 3; c++) { a.p[c] = nullptr; a.v[c] = nullptr; }
@@ -345,17 +349,19 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         a.check = check;
-        if (three) {
-            k_tgv_dual<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-            k_tgv_primal<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
-        } else {
-            k_tgv_dual<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-            k_tgv_primal<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
-        }
+        if (three) k_tgv_dual<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+        else k_tgv_dual<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
         CILREG_CUDA(cudaGetLastError());
+        if (T.use) {
+            CILREG_TRY(tgv_primal_stream_step(T, a, d, ctl.ctl(), ctl.partials(), s));
+        } else {
+            if (three) k_tgv_primal<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+            else k_tgv_primal<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
+            CILREG_CUDA(cudaGetLastError());
+        }
         note_launch(2);
         if (check) {
-            CILREG_TRY(ctl.after_check(it, num_blocks(L)));
+            CILREG_TRY(ctl.after_check(it, nparts));
             if (ctl.host_should_stop()) break;
         }
     }

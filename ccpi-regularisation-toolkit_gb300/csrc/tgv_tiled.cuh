@@ -1,0 +1,19 @@
+// TGV primal half-iteration as a 2.5D streaming kernel (tgv_tiled.cu).
+#pragma once
+
+#include "tgv_batch.cuh"
+
+namespace cilreg {
+
+struct TgvPlan {
+    dim3 grid, block;
+    long long nblocks = 0;
+    int zchunk = 0;
+    bool use = false;  // false: the per-voxel primal kernel of tgv.cu runs instead
+};
+
+TgvPlan tgv_primal_plan(const Dims& d);
+int tgv_primal_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, double2* partials,
+                           cudaStream_t s);
+
+}  // namespace cilreg

@@ -275,6 +275,25 @@ def test_sb_fused_sweeps_equal_per_sweep_kernels(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
+                                   (130, 33, 35)], ids=str)
+def test_tgv_streaming_primal_equals_per_voxel_kernel(shape, monkeypatch):
+    """The 2.5D streaming TGV primal kernel and the per-voxel one compute the
+    same iteration (and the same stopping iteration)."""
+    from ccpi.filters.regularisers import TGV
+
+    rng = np.random.default_rng(31 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil in (1e-3, 0.0):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = TGV(x, 0.05, 1.0, 2.0, 70, 12.0, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_TGV_KERNEL", "simple")
+        b = TGV(x, 0.05, 1.0, 2.0, 70, 12.0, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_TGV_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
 @pytest.mark.parametrize("shape", [(48, 61), (10, 16, 22), (70, 33, 35)], ids=str)
 def test_rof_per_voxel_lambda_matches_oracle(shape, monkeypatch):
     """ROF with a per-voxel lambda map (ROF_TV_core.c:280 lambda_is_arr) through the
