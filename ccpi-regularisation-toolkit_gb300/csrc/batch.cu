@@ -24,6 +24,7 @@
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
 #include "tgv_batch.cuh"
+#include "tgv_tiled.cuh"
 
 namespace cilreg {
 namespace {
@@ -332,8 +333,14 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
     const int np = L.three ? 3 : 2, nq = L.three ? 6 : 3;
     const float tau = (float)pow((double)L2, -0.5);  // TGV_core.c:54-55
 
+    // primal half: the streaming kernel (tgv_tiled.cu) unless
+    // CILREG_TGV_KERNEL=simple or a volume has 2^31 voxels or more
+    const char* ek = getenv("CILREG_TGV_KERNEL");
+    bool stream_primal = !(ek && ek[0] == 's');
+    for (int v = 0; v < nvol; v++)
+        if (L.dims[v].n >= (1LL << 31)) stream_primal = false;
     std::vector<TgvBatchVol> vols(nvol);
-    long long ntiles = 0;
+    long long ntiles = 0, nptiles = 0;
     size_t state_floats = 0;
     for (int v = 0; v < nvol; v++) {
         const Launch3 P = plan_launch(L.dims[v]);
@@ -345,18 +352,30 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
         V.kz = P.kz;
         V.tile_base = ntiles;
         ntiles += (long long)V.gx * V.gy * V.gz;
+        if (stream_primal) {
+            tgv_primal_tiles(V.d, V.pgx, V.pgy, V.pgz, V.pzc);
+        } else {
+            V.pgx = V.gx;
+            V.pgy = V.gy;
+            V.pgz = V.gz;
+            V.pzc = V.kz;
+        }
+        V.ptile_base = nptiles;
+        nptiles += (long long)V.pgx * V.pgy * V.pgz;
         state_floats += align256(sizeof(float) * (size_t)V.d.n) / sizeof(float) * (2 * np + nq);
     }
     float* state = (float*)sc.bytes(sizeof(float) * state_floats);
-    double2* part = (double2*)sc.bytes(sizeof(double2) * (size_t)ntiles);
+    double2* part = (double2*)sc.bytes(sizeof(double2) * (size_t)nptiles);
     StopCtl* d_ctl = (StopCtl*)sc.bytes(sizeof(StopCtl) * nvol);
     TgvBatchVol* d_vols = (TgvBatchVol*)sc.bytes(sizeof(TgvBatchVol) * nvol);
     int* d_tile_vol = (int*)sc.bytes(sizeof(int) * (size_t)ntiles);
+    int* d_ptile_vol = stream_primal ? (int*)sc.bytes(sizeof(int) * (size_t)nptiles) : nullptr;
     CheckSlot* d_slots = (CheckSlot*)sc.bytes(sizeof(CheckSlot) * nvol);
     StopCtl** d_ctlp = (StopCtl**)sc.bytes(sizeof(StopCtl*) * nvol);
-    if (!state || !part || !d_ctl || !d_vols || !d_tile_vol || !d_slots || !d_ctlp) return sc.status();
+    if (!state || !part || !d_ctl || !d_vols || !d_tile_vol || !d_slots || !d_ctlp || (stream_primal && !d_ptile_vol))
+        return sc.status();
     CILREG_CUDA(cudaMemsetAsync(state, 0, sizeof(float) * state_floats, s));
-    std::vector<int> tile_vol(ntiles);
+    std::vector<int> tile_vol(ntiles), ptile_vol(stream_primal ? nptiles : 0);
     std::vector<CheckSlot> slots(nvol);
     std::vector<StopCtl*> ctlp(nvol);
     float* r = state;
@@ -379,15 +398,21 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
         a.inv_lt = 1.0f / (a.lambda + tau);
         a.check = 0;
         V.ctl = d_ctl + v;
-        V.partials = part + V.tile_base;
+        V.partials = part + V.ptile_base;
         const long long nt = (long long)V.gx * V.gy * V.gz;
         for (long long t = 0; t < nt; t++) tile_vol[V.tile_base + t] = v;
-        slots[v] = CheckSlot{V.partials, nt, V.ctl};
+        const long long npt = (long long)V.pgx * V.pgy * V.pgz;
+        if (stream_primal)
+            for (long long t = 0; t < npt; t++) ptile_vol[V.ptile_base + t] = v;
+        slots[v] = CheckSlot{V.partials, npt, V.ctl};
         ctlp[v] = V.ctl;
         CILREG_CUDA(cudaMemcpyAsync(u[v], f[v], sizeof(float) * (size_t)V.d.n, cudaMemcpyDeviceToDevice, s));
     }
     CILREG_CUDA(cudaMemcpyAsync(d_vols, vols.data(), sizeof(TgvBatchVol) * nvol, cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaMemcpyAsync(d_tile_vol, tile_vol.data(), sizeof(int) * (size_t)ntiles, cudaMemcpyHostToDevice, s));
+    if (stream_primal)
+        CILREG_CUDA(cudaMemcpyAsync(d_ptile_vol, ptile_vol.data(), sizeof(int) * (size_t)nptiles,
+                                    cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaMemcpyAsync(d_slots, slots.data(), sizeof(CheckSlot) * nvol, cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaMemcpyAsync(d_ctlp, ctlp.data(), sizeof(StopCtl*) * nvol, cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaStreamSynchronize(s));
@@ -395,7 +420,7 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
     auto enqueue = [&]() -> int {
         for (int it = 0; it < iters; it++) {
             const int check = (epsil != 0.0f && it % 5 == 0) ? 1 : 0;
-            CILREG_TRY(tgv_batch_step(d_vols, d_tile_vol, ntiles, L.three, check, s));
+            CILREG_TRY(tgv_batch_step(d_vols, d_tile_vol, ntiles, d_ptile_vol, nptiles, L.three, check, s));
             note_launch(2);
             if (check) CILREG_TRY(launch_finalize_batch(d_slots, nvol, epsil, it, s));
         }

@@ -296,17 +296,16 @@ __global__ void __launch_bounds__(256, 4) k_tgv_primal_batch(const TgvBatchVol* 
 
 }  // namespace
 
-int tgv_batch_step(const TgvBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int check,
-                   cudaStream_t s) {
+int tgv_batch_step(const TgvBatchVol* d_vols, const int* d_tile_vol, long long ntiles, const int* d_ptile_vol,
+                   long long nptiles, bool three, int check, cudaStream_t s) {
     if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
     const dim3 grid((unsigned)ntiles), block(32, 8, 1);
-    if (three) {
-        k_tgv_dual_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
-        k_tgv_primal_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
-    } else {
-        k_tgv_dual_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
-        k_tgv_primal_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
-    }
+    if (three) k_tgv_dual_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
+    else k_tgv_dual_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
+    CILREG_CUDA(cudaGetLastError());
+    if (d_ptile_vol) return tgv_primal_batch_step(d_vols, d_ptile_vol, nptiles, three, check, s);
+    if (three) k_tgv_primal_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
+    else k_tgv_primal_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

@@ -34,29 +34,79 @@ __device__ __forceinline__ float bwd(float x, float xprev, bool first, bool last
     return first ? x : (last ? -xprev : x - xprev);
 }
 
-template <bool THREE, bool CHECK>
-__global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, int zc, const StopCtl* ctl,
-                                                             double2* partials) {
+__device__ __forceinline__ void publish_args(const TgvArgs& a, float* volatile* tab, float* sc) {
+    for (int i = 0; i < 3; i++) tab[i] = a.p[i];
+    for (int i = 0; i < 6; i++) tab[3 + i] = a.q[i];
+    for (int i = 0; i < 3; i++) tab[9 + i] = a.v[i];
+    tab[12] = a.u;
+    tab[13] = const_cast<float*>(a.u0);
+    sc[0] = a.tau;
+    sc[1] = a.lambda;
+    sc[2] = a.inv_lt;
+}
+
+// BATCH: one flat grid over the tiles of every volume of a batched run
+// (TgvBatchVol::pgx.. describe a volume's tiles); otherwise one volume.  The
+// CTA copies its volume's arguments to shared memory first, so the state
+// pointers are read from there rather than held in registers.
+template <bool THREE, bool CHECK, bool BATCH>
+__global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a1, Dims d1, int zc1, const StopCtl* ctl1,
+                                                             double2* partials1, const TgvBatchVol* __restrict__ vols,
+                                                             const int* __restrict__ tile_vol) {
     // x/y predecessors: 3D P1 P2 Q1 Q2 Q4 Q5 Q6; 2D P1 P2 Q1 Q2 Q3
     constexpr int NS = THREE ? 7 : 5;
     __shared__ float sm[2][NS][BY * BX];
+    // state pointers, read from shared memory at each use (volatile: not held
+    // in registers across the loop); 0-2 P, 3-8 Q, 9-11 V, 12 U, 13 U0
+    __shared__ float* volatile tab[14];
+    __shared__ float sc[3];  // tau, lambda, 1 / (lambda + tau)
+    int bx, by, bz, zc;
+    Dims d;
+    const StopCtl* ctl;
+    double2* partials;
+    long long slot;
+    if constexpr (BATCH) {
+        const long long t = blockIdx.x;
+        const TgvBatchVol& V = vols[tile_vol[t]];
+        const long long lt = t - V.ptile_base;
+        bx = (int)(lt % V.pgx);
+        by = (int)((lt / V.pgx) % V.pgy);
+        bz = (int)(lt / ((long long)V.pgx * V.pgy));
+        d = V.d;
+        zc = V.pzc;
+        ctl = V.ctl;
+        partials = V.partials;
+        slot = lt;
+        if (threadIdx.x == 0 && threadIdx.y == 0) publish_args(V.args, tab, sc);
+    } else {
+        bx = blockIdx.x;
+        by = blockIdx.y;
+        bz = blockIdx.z;
+        d = d1;
+        zc = zc1;
+        ctl = ctl1;
+        partials = partials1;
+        slot = block_slot();
+        if (threadIdx.x == 0 && threadIdx.y == 0) publish_args(a1, tab, sc);
+    }
     if (ctl->stop) return;
+    __syncthreads();
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int x = blockIdx.x * OX + tx - 1;
-    const int y = blockIdx.y * OY + ty - 1;
+    const int x = bx * OX + tx - 1;
+    const int y = by * OY + ty - 1;
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
     const bool o_pt = in_xy && tx >= 1 && ty >= 1;
     const bool xf = (x == 0), xl = (x == nx - 1), yf = (y == 0), yl = (y == ny - 1);
     const int oc = ty * BX + tx;
     const int ox = ty * BX + max(tx - 1, 0), oy = max(ty - 1, 0) * BX + tx;
     const int col = min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
-    const float tau = a.tau, lam = a.lambda, ilt = a.inv_lt;
+    const float tau = sc[0], lam = sc[1], ilt = sc[2];
     float pa = 0.f, pb = 0.f;
 
     if constexpr (!THREE) {
-        const float p1 = __ldg(a.p[0] + col), p2 = __ldg(a.p[1] + col);
-        const float q1 = __ldg(a.q[0] + col), q2 = __ldg(a.q[1] + col), q3 = __ldg(a.q[2] + col);
+        const float p1 = __ldg(tab[0] + col), p2 = __ldg(tab[1] + col);
+        const float q1 = __ldg(tab[3 + 0] + col), q2 = __ldg(tab[3 + 1] + col), q3 = __ldg(tab[3 + 2] + col);
         sm[0][0][oc] = p1;
         sm[0][1][oc] = p2;
         sm[0][2][oc] = q1;
@@ -66,10 +116,10 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, 
         if (o_pt) {
             // DivProjP_2D + newU (TGV_core.c:277-298, 300-306)
             const float dv = bwd(p1, sm[0][0][ox], xf, xl) + bwd(p2, sm[0][1][oy], yf, yl);
-            const float uo = a.u[col];
-            const float un = (lam * (uo + tau * dv) + tau * __ldg(a.u0 + col)) * ilt;
+            const float uo = tab[12][col];
+            const float un = (lam * (uo + tau * dv) + tau * __ldg(tab[13] + col)) * ilt;
             const float ue = 2.0f * un - uo;
-            a.u[col] = ue;
+            tab[12][col] = ue;
             if (CHECK) {
                 const float df = ue - uo;
                 pa = df * df;
@@ -78,29 +128,29 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, 
             // UpdV_2D + newV (TGV_core.c:308-345)
             const float d1 = bwd(q1, sm[0][2][ox], xf, xl) + bwd(q3, sm[0][4][oy], yf, yl);
             const float d2 = bwd(q3, sm[0][4][ox], xf, xl) + bwd(q2, sm[0][3][oy], yf, yl);
-            const float v1 = a.v[0][col], v2 = a.v[1][col];
-            a.v[0][col] = 2.0f * (v1 + tau * (p1 + d1)) - v1;
-            a.v[1][col] = 2.0f * (v2 + tau * (p2 + d2)) - v2;
+            const float v1 = tab[9 + 0][col], v2 = tab[9 + 1][col];
+            tab[9 + 0][col] = 2.0f * (v1 + tau * (p1 + d1)) - v1;
+            tab[9 + 1][col] = 2.0f * (v2 + tau * (p2 + d2)) - v2;
         }
     } else {
-        const int z0 = blockIdx.z * zc;
+        const int z0 = bz * zc;
         const int z1 = min(z0 + zc, nz);
         const int sxy = (int)d.sxy;
         auto at = [&](int k) -> int { return min(max(k, 0), nz - 1) * sxy + col; };
         // z predecessors (plane k-1): P3, Q3, Q5, Q6
         const int om = at(z0 - 1);
-        float zp3 = __ldg(a.p[2] + om), zq3 = __ldg(a.q[2] + om), zq5 = __ldg(a.q[4] + om),
-              zq6 = __ldg(a.q[5] + om);
+        float zp3 = __ldg(tab[2] + om), zq3 = __ldg(tab[3 + 2] + om), zq5 = __ldg(tab[3 + 4] + om),
+              zq6 = __ldg(tab[3 + 5] + om);
         // plane k: P1..3, Q1..6 (every thread); U, U0, V1..3 (updated voxels)
         float c[9], cu = 0.f, cu0 = 0.f, cv[3] = {0.f, 0.f, 0.f};
         auto load = [&](int k, float* pq, float& u, float& u0, float* vv) {
             const int o = at(k);
-            for (int i = 0; i < 3; i++) pq[i] = __ldg(a.p[i] + o);
-            for (int i = 0; i < 6; i++) pq[3 + i] = __ldg(a.q[i] + o);
+            for (int i = 0; i < 3; i++) pq[i] = __ldg(tab[i] + o);
+            for (int i = 0; i < 6; i++) pq[3 + i] = __ldg(tab[3 + i] + o);
             if (o_pt) {
-                u = a.u[o];
-                u0 = __ldg(a.u0 + o);
-                for (int i = 0; i < 3; i++) vv[i] = a.v[i][o];
+                u = tab[12][o];
+                u0 = __ldg(tab[13] + o);
+                for (int i = 0; i < 3; i++) vv[i] = tab[9 + i][o];
             }
         };
         load(z0, c, cu, cu0, cv);
@@ -126,7 +176,7 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, 
                 const float un = (lam * (cu + tau * dv) + tau * cu0) * ilt;
                 const float ue = 2.0f * un - cu;
                 const int o = k * sxy + col;
-                a.u[o] = ue;
+                tab[12][o] = ue;
                 if (CHECK) {
                     const float df = ue - cu;
                     pa += df * df;
@@ -139,9 +189,9 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, 
                             q6y = bwd(c[8], sm[S][6][oy], yf, yl);
                 const float q6z = bwd(c[8], zq6, zf, zl), q5z = bwd(c[7], zq5, zf, zl), q3 = bwd(c[5], zq3, zf, zl);
                 const float d1 = q1 + q4y + q5z, d2 = q4x + q2 + q6z, d3 = q5x + q6y + q3;
-                a.v[0][o] = 2.0f * (cv[0] + tau * (c[0] + d1)) - cv[0];
-                a.v[1][o] = 2.0f * (cv[1] + tau * (c[1] + d2)) - cv[1];
-                a.v[2][o] = 2.0f * (cv[2] + tau * (c[2] + d3)) - cv[2];
+                tab[9 + 0][o] = 2.0f * (cv[0] + tau * (c[0] + d1)) - cv[0];
+                tab[9 + 1][o] = 2.0f * (cv[1] + tau * (c[1] + d2)) - cv[1];
+                tab[9 + 2][o] = 2.0f * (cv[2] + tau * (c[2] + d3)) - cv[2];
             }
             zp3 = c[2];
             zq3 = c[5];
@@ -159,7 +209,7 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a, Dims d, 
         }
         if (k < z1) step(Ic<0>{}, k);
     }
-    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, slot);
 }
 
 }  // namespace
@@ -172,7 +222,7 @@ TgvPlan tgv_primal_plan(const Dims& d) {
     T.use = !(e && e[0] == 's') && d.n < (1LL << 31);
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
-        static const int resident = resident_ctas(k_tgv_primal_stream<true, false>, NT);
+        static const int resident = resident_ctas(k_tgv_primal_stream<true, false, false>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
         T.zchunk = wave_zchunk(tiles, d.nz, resident, 0, ZCHUNK);
     } else {
@@ -186,9 +236,27 @@ TgvPlan tgv_primal_plan(const Dims& d) {
 int tgv_primal_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, double2* partials,
                            cudaStream_t s) {
     const bool three = d.nz > 1;
-    auto kern = three ? (a.check ? k_tgv_primal_stream<true, true> : k_tgv_primal_stream<true, false>)
-                      : (a.check ? k_tgv_primal_stream<false, true> : k_tgv_primal_stream<false, false>);
-    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+    auto kern = three ? (a.check ? k_tgv_primal_stream<true, true, false> : k_tgv_primal_stream<true, false, false>)
+                      : (a.check ? k_tgv_primal_stream<false, true, false> : k_tgv_primal_stream<false, false, false>);
+    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials, nullptr, nullptr);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc) {
+    zc = (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1;
+    gx = (d.nx + OX - 1) / OX;
+    gy = (d.ny + OY - 1) / OY;
+    gz = (d.nz + zc - 1) / zc;
+}
+
+int tgv_primal_batch_step(const TgvBatchVol* d_vols, const int* d_ptile_vol, long long nptiles, bool three, int check,
+                          cudaStream_t s) {
+    if (nptiles < 1 || nptiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", nptiles);
+    auto kern = three ? (check ? k_tgv_primal_stream<true, true, true> : k_tgv_primal_stream<true, false, true>)
+                      : (check ? k_tgv_primal_stream<false, true, true> : k_tgv_primal_stream<false, false, true>);
+    TgvArgs none{};
+    kern<<<dim3((unsigned)nptiles), dim3(BX, BY, 1), 0, s>>>(none, Dims{}, 1, nullptr, nullptr, d_vols, d_ptile_vol);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

@@ -16,4 +16,11 @@ TgvPlan tgv_primal_plan(const Dims& d);
 int tgv_primal_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, double2* partials,
                            cudaStream_t s);
 
+// tiling of the streaming primal kernel in a batched run (64-plane chunks)
+void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);
+// primal half-iteration of every volume of a batch: one flat grid over the
+// volumes' streaming tiles (TgvBatchVol::ptile_base.., tile -> volume map)
+int tgv_primal_batch_step(const TgvBatchVol* d_vols, const int* d_ptile_vol, long long nptiles, bool three, int check,
+                          cudaStream_t s);
+
 }  // namespace cilreg
