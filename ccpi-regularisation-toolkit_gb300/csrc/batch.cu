@@ -130,6 +130,7 @@ struct FgpBatch {
     float* ring = nullptr;
     size_t ring_bytes = 0;
     long long ntiles = 0;
+    bool wide = false;  // some volume has 2^31 voxels or more
 };
 
 int fgp_build(FgpBatch& B, Scratch& sc, const BatchLayout& L, const float* const* f, float* const* u,
@@ -143,6 +144,7 @@ int fgp_build(FgpBatch& B, Scratch& sc, const BatchLayout& L, const float* const
         const Dims& d = L.dims[v];
         FgpBatchVol& V = B.vols[v];
         V.d = d;
+        if (d.n >= (1LL << 31)) B.wide = true;
         V.zc = zc_override > 0 ? (d.nz > 1 ? (zc_override < d.nz ? zc_override : d.nz) : 1) : fgp_default_zchunk(d);
         fgp_tile_grid(d, V.zc, V.gx, V.gy, V.gz);
         V.tile_base = B.ntiles;
@@ -208,7 +210,7 @@ int fgp_enqueue(FgpBatch& B, int nvol, bool three, int iters, float epsil, int m
         const int check = (checking && it % 5 == 0) ? 1 : 0;
         const int write_u = (it == iters - 1) || check || (checking && (it + 1) % 5 == 0);
         const int write_p = (it != iters - 1);
-        CILREG_TRY(fgp_batch_step(B.d_vols, B.d_tile_vol, B.ntiles, three, it, cprev, nonneg == 1, methodTV != 0,
+        CILREG_TRY(fgp_batch_step(B.d_vols, B.d_tile_vol, B.ntiles, three, B.wide, it, cprev, nonneg == 1, methodTV != 0,
                                   write_u, write_p, check, s));
         note_launch();
         const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;  // FGP_TV_core.c:138

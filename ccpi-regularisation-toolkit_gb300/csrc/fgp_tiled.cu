@@ -13,8 +13,9 @@
 //   3. one plane behind, forms P^k(k-1) from U's forward differences: x/y
 //      from the previous U plane in shared memory, z from the U_k just made
 //      (FGP_TV_core.c:237-256), then projects it (utils.c:180-213).
-// R and U are formed once per voxel, with 32-bit tile indexing, two barriers
-// per plane and no integer division.  Global traffic is the fused
+// R and U are formed once per voxel, with 32-bit tile indexing and element
+// offsets (below 2^31 voxels), two barriers per plane and no integer division;
+// the stopping-check work is compiled only into the check-iteration variant.  Global traffic is the fused
 // iteration's 40 B/voxel; the one-voxel halo ring (15% of the tile) is re-read
 // from L2.
 #include "fgp_tiled.cuh"
@@ -40,9 +41,10 @@ struct TiledArgs {
     int nonneg, aniso, write_u, write_p, check;
 };
 
-// One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk.  The
-// caller reduces the returned per-thread sums when a.check is set.
-template <bool THREE>
+// One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk.
+// CHECK: a stopping check (reads U_prev; the caller reduces the returned
+// per-thread sums).  IT: element-offset type (int below 2^31 voxels).
+template <bool THREE, bool CHECK, typename IT>
 __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& d, int zc, int bx, int by, int bz,
                                                 float& pa_out, float& pb_out) {
     __shared__ float sR1[BY][BX];
@@ -57,13 +59,14 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
     const bool u_pt = in_xy && tx >= 1 && ty >= 1;                    // U needed here
     const bool p_pt = u_pt && tx <= OX && ty <= OY;                    // P written here
-    const long long col = in_xy ? ((long long)y * nx + x) : 0;
+    const IT col = in_xy ? ((IT)y * nx + x) : 0;
+    const IT sxy = (IT)d.sxy;
 
     // prefetch registers for one plane
     float c1 = 0.f, o1 = 0.f, c2 = 0.f, o2 = 0.f, c3 = 0.f, o3 = 0.f, fv = 0.f;
     auto load_plane = [&](int k) {
         if (in_xy && k >= 0 && k < nz) {
-            const long long v = (long long)k * d.sxy + col;
+            const IT v = (IT)k * sxy + col;
             c1 = __ldg(a.pc[0] + v);
             o1 = __ldg(a.po[0] + v);
             c2 = __ldg(a.pc[1] + v);
@@ -92,7 +95,7 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
         // U_prev of plane k, consumed one plane later: loaded here so that its
         // latency overlaps the barriers instead of stalling the P step
         float uo_next = 0.f;
-        if (a.check && p_pt && k >= z0 && k < z1) uo_next = a.u[(long long)k * d.sxy + col];
+        if (CHECK && p_pt && k >= z0 && k < z1) uo_next = a.u[(IT)k * sxy + col];
         sR1[ty][tx] = r1;
         sR2[ty][tx] = r2;
         __syncthreads();
@@ -112,8 +115,8 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
         // 3. P^k of plane k-1
         const int kp = k - 1;
         if (p_pt && kp >= z0) {
-            const long long v = (long long)kp * d.sxy + col;
-            if (a.check) {
+            const IT v = (IT)kp * sxy + col;
+            if (CHECK) {
                 const float df = up - uo;
                 pa += df * df;
                 pb += up * up;
@@ -132,12 +135,10 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
                 }
                 if (!a.aniso) {
                     const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
-                    if (den > 1.f) {
-                        const float sq = rsqrtf(den);  // within 2 ulp of 1/sqrtf
-                        p1 = p1 * sq;
-                        p2 = p2 * sq;
-                        p3 = p3 * sq;
-                    }
+                    const float sq = (den > 1.f) ? rsqrtf(den) : 1.f;  // within 2 ulp of 1/sqrtf
+                    p1 = p1 * sq;
+                    p2 = p2 * sq;
+                    p3 = p3 * sq;
                 } else {
                     p1 = p1 / fmaxf(fabsf(p1), 1.f);
                     p2 = p2 / fmaxf(fabsf(p2), 1.f);
@@ -158,20 +159,19 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
     pb_out = pb;
 }
 
-template <bool THREE>
+template <bool THREE, bool CHECK, typename IT>
 __global__ void __launch_bounds__(NT, 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
                                                       double2* partials) {
     if (ctl->stop) return;
     float pa = 0.f, pb = 0.f;
-    fgp_stream_tile<THREE>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
-    if (a.check) block_pair_partial<NT>(pa, pb, partials, block_slot());
+    fgp_stream_tile<THREE, CHECK, IT>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
-template <bool THREE>
+template <bool THREE, bool CHECK, typename IT>
 __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* __restrict__ vols,
                                                             const int* __restrict__ tile_vol, int it, float c,
-                                                            int nonneg, int aniso, int write_u, int write_p,
-                                                            int check) {
+                                                            int nonneg, int aniso, int write_u, int write_p) {
     const long long t = blockIdx.x;
     const FgpBatchVol& V = vols[tile_vol[t]];
     if (V.ctl->stop) return;
@@ -194,10 +194,10 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* _
     a.aniso = aniso;
     a.write_u = write_u;
     a.write_p = write_p;
-    a.check = check;
+    a.check = CHECK;
     float pa = 0.f, pb = 0.f;
-    fgp_stream_tile<THREE>(a, V.d, V.zc, bx, by, bz, pa, pb);
-    if (check) block_pair_partial<NT>(pa, pb, V.partials, lt);
+    fgp_stream_tile<THREE, CHECK, IT>(a, V.d, V.zc, bx, by, bz, pa, pb);
+    if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
 }
 
 }  // namespace
@@ -208,17 +208,20 @@ void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz) {
     gz = (d.nz + zc - 1) / zc;
 }
 
-int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int it, float c,
-                   int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s) {
+int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, bool wide, int it,
+                   float c, int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s) {
     if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
     const dim3 grid((unsigned)ntiles);  // one CTA per tile of every volume
     const dim3 block(BX, BY, 1);
-    if (three)
-        k_fgp_stream_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p,
-                                                        check);
+    decltype(&k_fgp_stream_batch<true, true, int>) kern;
+    if (!wide)
+        kern = three ? (check ? k_fgp_stream_batch<true, true, int> : k_fgp_stream_batch<true, false, int>)
+                     : (check ? k_fgp_stream_batch<false, true, int> : k_fgp_stream_batch<false, false, int>);
     else
-        k_fgp_stream_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p,
-                                                         check);
+        kern = three ? (check ? k_fgp_stream_batch<true, true, long long> : k_fgp_stream_batch<true, false, long long>)
+                     : (check ? k_fgp_stream_batch<false, true, long long>
+                              : k_fgp_stream_batch<false, false, long long>);
+    kern<<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }
@@ -233,7 +236,7 @@ TiledPlan fgp_tiled_plan(const Dims& d) {
     if (d.nz > 1) {
         // one volume: balance the CTAs over the SMs (the batched path packs
         // many volumes and keeps fgp_default_zchunk)
-        static const int resident = resident_ctas(k_fgp_stream<true>, NT);
+        static const int resident = resident_ctas(k_fgp_stream<true, false, int>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
         T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
     } else {
@@ -263,10 +266,15 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
     a.write_u = write_u;
     a.write_p = write_p;
     a.check = check;
-    if (d.nz > 1)
-        k_fgp_stream<true><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+    const bool three = d.nz > 1;
+    decltype(&k_fgp_stream<true, true, int>) kern;
+    if (d.n < (1LL << 31))
+        kern = three ? (check ? k_fgp_stream<true, true, int> : k_fgp_stream<true, false, int>)
+                     : (check ? k_fgp_stream<false, true, int> : k_fgp_stream<false, false, int>);
     else
-        k_fgp_stream<false><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+        kern = three ? (check ? k_fgp_stream<true, true, long long> : k_fgp_stream<true, false, long long>)
+                     : (check ? k_fgp_stream<false, true, long long> : k_fgp_stream<false, false, long long>);
+    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

@@ -36,8 +36,9 @@ struct FgpBatchVol {
 void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz);
 
 // one iteration `it` of every volume: flat grid over all tiles, tile_vol maps
-// a flat tile to its volume; all volumes share dimensionality `three`
-int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, int it, float c,
-                   int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s);
+// a flat tile to its volume; all volumes share dimensionality `three`; `wide`
+// when some volume has 2^31 voxels or more (64-bit element offsets)
+int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, bool wide, int it,
+                   float c, int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s);
 
 }  // namespace cilreg
