@@ -13,6 +13,8 @@
 //      x/y from shared memory).
 // One barrier per plane.  HBM traffic: read U and f, write U (12 B/voxel);
 // the reference's two sweeps move 24 B and store W.
+#include <type_traits>
+
 #include "diff4th_tiled.cuh"
 
 namespace cilreg {
@@ -24,11 +26,15 @@ constexpr int OX = BX - 4, OY = BY - 4;
 constexpr int NT = BX * BY;
 constexpr int ZCHUNK = 64;
 
-template <bool THREE>
+template <int V>
+using Ic = std::integral_constant<int, V>;
+
+// CHECK: a stopping-check iteration (per-CTA partial sums).  IT: element-offset
+// type (int below 2^31 voxels).
+template <bool THREE, bool CHECK, typename IT>
 __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                      const float* __restrict__ F, float lam, float tau, float isg2,
-                                                     Dims d, int zc, const StopCtl* ctl, int check,
-                                                     double2* partials) {
+                                                     Dims d, int zc, const StopCtl* ctl, double2* partials) {
     __shared__ float sU[4][BY][BX];
     __shared__ float sW[2][BY][BX];
     if (ctl->stop) return;
@@ -46,24 +52,29 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
     const int xl = (nx == 1) ? tx : ((x - 1 < 0) ? tx + 1 : tx - 1);
     const int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
     const int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
-    const long long col = in_xy ? ((long long)y * nx + x) : 0;
+    const IT col = in_xy ? ((IT)y * nx + x) : 0;
+    const IT sxy = (IT)d.sxy;
     auto ld = [&](const float* p, int k) -> float {
-        return (in_xy && k >= 0 && k < nz) ? __ldg(p + (long long)k * d.sxy + col) : 0.f;
+        return (in_xy && k >= 0 && k < nz) ? __ldg(p + ((IT)k * sxy + col)) : 0.f;
     };
-    auto ring = [](int k) { return (k + 4) & 3; };
 
     float wa = 0.f, wb = 0.f, wc = 0.f;  // W of planes j-1, j-2, j-3 at this voxel
     float pa = 0.f, pb = 0.f;
-    sU[ring(z0 - 2)][ty][tx] = ld(U, z0 - 2);
-    sU[ring(z0 - 1)][ty][tx] = ld(U, z0 - 1);
+    // U ring slot of plane p: (p - z0 + 4) & 3; W ring slot: (p - z0 + 2) & 1
+    sU[2][ty][tx] = ld(U, z0 - 2);
+    sU[3][ty][tx] = ld(U, z0 - 1);
     float uj = ld(U, z0);
     float fa = o_pt ? ld(F, z0 - 2) : 0.f, fb = o_pt ? ld(F, z0 - 1) : 0.f;  // f of planes j-2, j-1
 
-    for (int j = z0; j <= z1 + 1; ++j) {
+    // R = (j - z0) & 3
+    auto step = [&](auto rr, int j) {
+        constexpr int R = decltype(rr)::value;
+        constexpr int SJ = R, SM = (R + 3) & 3, SM2 = (R + 2) & 3;  // U slots of planes j, j-1, j-2
+        constexpr int WM = (R + 1) & 1, WK = R & 1;                 // W slots of planes j-1, j-2
         const float un1 = (j + 1 <= z1 + 1) ? ld(U, j + 1) : 0.f;  // prefetch U(j+1)
         const float fn = o_pt ? ld(F, j) : 0.f;                      // prefetch f(j)
         // B. publish U(j)
-        sU[ring(j)][ty][tx] = uj;
+        sU[SJ][ty][tx] = uj;
         __syncthreads();
         // A. weighted Laplacian of plane m = j-1 (Diffus4th_order_core.c:176-235)
         const int m = j - 1;
@@ -71,26 +82,26 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
         wb = wa;
         wa = 0.f;
         if (m >= 0 && m < nz && m >= z0 - 1 && m <= z1 && w_pt) {
-            const int s0 = ring(m);
-            const float c0 = sU[s0][ty][tx];
-            const float um_x = sU[s0][ty][xl], up_x = sU[s0][ty][xh];
-            const float um_y = sU[s0][yl][tx], up_y = sU[s0][yh][tx];
+            const float c0 = sU[SM][ty][tx];
+            const float um_x = sU[SM][ty][xl], up_x = sU[SM][ty][xh];
+            const float um_y = sU[SM][yl][tx], up_y = sU[SM][yh][tx];
             const float gx = 0.5f * (um_x - up_x), gy = 0.5f * (um_y - up_y);
             const float gx2 = gx * gx, gy2 = gy * gy;
             const float gxx = um_x + up_x - 2.0f * c0;
             const float gyy = um_y + up_y - 2.0f * c0;
-            const float gxy = 0.25f * (sU[s0][yl][xl] + sU[s0][yh][xh] - sU[s0][yh][xl] - sU[s0][yl][xh]);
+            const float gxy = 0.25f * (sU[SM][yl][xl] + sU[SM][yh][xh] - sU[SM][yh][xl] - sU[SM][yl][xh]);
             const float xy2 = 2.0f * gx * gy * gxy;
             float den, vn, vo;
             if (THREE) {
-                const int sl = (nz == 1) ? s0 : ((m == 0) ? ring(m + 1) : ring(m - 1));       // mirrored k-1
-                const int sh = (nz == 1) ? s0 : ((m == nz - 1) ? ring(m - 1) : ring(m + 1));  // mirrored k+1
-                const float zm = sU[sl][ty][tx], zp = sU[sh][ty][tx];
+                // mirrored k-1 / k+1 planes (an axis of length 1 maps to itself)
+                const float(*pl)[BX] = (nz == 1) ? sU[SM] : ((m == 0) ? sU[SJ] : sU[SM2]);
+                const float(*ph)[BX] = (nz == 1) ? sU[SM] : ((m == nz - 1) ? sU[SM2] : sU[SJ]);
+                const float zm = pl[ty][tx], zp = ph[ty][tx];
                 const float gz = 0.5f * (zm - zp);
                 const float gz2 = gz * gz;
                 const float gzz = zm + zp - 2.0f * c0;
-                const float gxz = 0.25f * (sU[sl][ty][xl] - sU[sl][ty][xh] - sU[sh][ty][xl] + sU[sh][ty][xh]);
-                const float gyz = 0.25f * (sU[sl][yl][tx] - sU[sl][yh][tx] - sU[sh][yl][tx] + sU[sh][yh][tx]);
+                const float gxz = 0.25f * (pl[ty][xl] - pl[ty][xh] - ph[ty][xl] + ph[ty][xh]);
+                const float gyz = 0.25f * (pl[yl][tx] - pl[yh][tx] - ph[yl][tx] + ph[yh][tx]);
                 const float xz2 = 2.0f * gx * gz * gxz;
                 const float yz2 = 2.0f * gy * gz * gyz;
                 den = gx2 + gy2 + gz2;
@@ -109,26 +120,25 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
             }
             const float c = __frcp_rn(1.0f + den * isg2);
             wa = (c * c) * vn + c * vo;
-            sW[m & 1][ty][tx] = wa;
+            sW[WM][ty][tx] = wa;
         }
         // C. update plane kf = j-2 (Diffus4th_order_core.c:237-265); its W was
         // published in the previous step
         const int kf = j - 2;
         if (o_pt && kf >= z0 && kf < z1) {
-            const int sk = kf & 1;
-            const float w = sW[sk][ty][tx];
-            const float lx = sW[sk][ty][xl] + sW[sk][ty][xh] - 2.0f * w;
-            const float ly = sW[sk][yl][tx] + sW[sk][yh][tx] - 2.0f * w;
+            const float w = sW[WK][ty][tx];
+            const float lx = sW[WK][ty][xl] + sW[WK][ty][xh] - 2.0f * w;
+            const float ly = sW[WK][yl][tx] + sW[WK][yh][tx] - 2.0f * w;
             float lap = lx + ly;
             if (THREE) {
                 const float wlo = (nz == 1) ? w : ((kf == 0) ? wa : wc);        // mirrored W(k-1)
                 const float whi = (nz == 1) ? w : ((kf == nz - 1) ? wc : wa);   // mirrored W(k+1)
                 lap = lap + (wlo + whi - 2.0f * w);
             }
-            const float u = sU[ring(kf)][ty][tx];
+            const float u = sU[SM2][ty][tx];
             const float un = u + tau * (-lam * lap - (u - fa));
-            Un[(long long)kf * d.sxy + col] = un;
-            if (check) {
+            Un[(IT)kf * sxy + col] = un;
+            if (CHECK) {
                 const float df = un - u;
                 pa += df * df;
                 pb += un * un;
@@ -137,8 +147,18 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
         uj = un1;
         fa = fb;
         fb = fn;
+    };
+    int j = z0;
+    for (; j + 3 <= z1 + 1; j += 4) {
+        step(Ic<0>{}, j);
+        step(Ic<1>{}, j + 1);
+        step(Ic<2>{}, j + 2);
+        step(Ic<3>{}, j + 3);
     }
-    if (check) block_pair_partial<NT>(pa, pb, partials, block_slot());
+    if (j <= z1 + 1) step(Ic<0>{}, j);
+    if (j + 1 <= z1 + 1) step(Ic<1>{}, j + 1);
+    if (j + 2 <= z1 + 1) step(Ic<2>{}, j + 2);
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
 }  // namespace
@@ -147,7 +167,7 @@ D4Plan d4_stream_plan(const Dims& d) {
     D4Plan T;
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
-        static const int resident = resident_ctas(k_d4_stream<true>, NT);
+        static const int resident = resident_ctas(k_d4_stream<true, false, int>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
         T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
     } else {
@@ -160,10 +180,15 @@ D4Plan d4_stream_plan(const Dims& d) {
 
 int d4_stream_step(const D4Plan& T, const float* cur, float* nxt, const float* f, float lam, float tau, float isg2,
                    const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
-    if (d.nz > 1)
-        k_d4_stream<true><<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, check, partials);
+    const bool three = d.nz > 1;
+    decltype(&k_d4_stream<true, true, int>) kern;
+    if (d.n < (1LL << 31))
+        kern = three ? (check ? k_d4_stream<true, true, int> : k_d4_stream<true, false, int>)
+                     : (check ? k_d4_stream<false, true, int> : k_d4_stream<false, false, int>);
     else
-        k_d4_stream<false><<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, check, partials);
+        kern = three ? (check ? k_d4_stream<true, true, long long> : k_d4_stream<true, false, long long>)
+                     : (check ? k_d4_stream<false, true, long long> : k_d4_stream<false, false, long long>);
+    kern<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, partials);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

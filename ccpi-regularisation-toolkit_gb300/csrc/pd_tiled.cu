@@ -26,8 +26,10 @@ constexpr int OX = BX - 2, OY = BY - 2;
 constexpr int NT = BX * BY;
 constexpr int ZCHUNK = 64;
 
-template <bool THREE>
-__global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int zc, const StopCtl* ctl,
+// CHECK: a stopping-check iteration (writes U before extrapolation and the
+// per-CTA partial sums).  IT: element-offset type (int below 2^31 voxels).
+template <bool THREE, bool CHECK, typename IT>
+__global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int zc, const StopCtl* ctl,
                                                      double2* partials) {
     __shared__ float sUe[2][BY][BX];
     __shared__ float sP1[2][BY][BX];
@@ -45,10 +47,11 @@ __global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int
     // mirrored forward neighbour inside the tile (length-1 axis -> itself)
     const int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
     const int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
-    const long long col = in_xy ? ((long long)y * nx + x) : 0;
+    const IT col = in_xy ? ((IT)y * nx + x) : 0;
+    const IT sxy = (IT)d.sxy;
 
     auto ld = [&](const float* p, int k) -> float {
-        return (in_xy && k >= 0 && k < nz) ? __ldg(p + (long long)k * d.sxy + col) : 0.f;
+        return (in_xy && k >= 0 && k < nz) ? __ldg(p + ((IT)k * sxy + col)) : 0.f;
     };
     // registers: Ue of planes j-2, j-1, j; prefetched Ue(j+1), old dual and f of plane j
     float um2 = ld(a.u, z0 - 2), um1 = ld(a.u, z0 - 1), uj = ld(a.u, z0);
@@ -79,12 +82,10 @@ __global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int
             }
             if (!a.aniso) {
                 const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
-                if (den > 1.f) {
-                    const float sq = rsqrtf(den);
-                    p1 *= sq;
-                    p2 *= sq;
-                    p3 *= sq;
-                }
+                const float sq = (den > 1.f) ? rsqrtf(den) : 1.f;
+                p1 *= sq;
+                p2 *= sq;
+                p3 *= sq;
             } else {
                 p1 = p1 / fmaxf(fabsf(p1), 1.f);
                 p2 = p2 / fmaxf(fabsf(p2), 1.f);
@@ -109,8 +110,8 @@ __global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int
             float uc = um1;
             if (a.nonneg && uc < 0.f) uc = 0.f;
             const float unew = (uc - a.tau * dv + a.lt * fq) * a.inv_onelt;
-            const long long v = (long long)k * d.sxy + col;
-            if (a.check) {
+            const IT v = (IT)k * sxy + col;
+            if (CHECK) {
                 const float df = unew - uc;
                 pa += df * df;
                 pb += unew * unew;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(NT, 2) k_pd_stream(PdStreamArgs a, Dims d, int
         q3 = nq3;
         fq = nf;
     }
-    if (a.check) block_pair_partial<NT>(pa, pb, partials, block_slot());
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
 }  // namespace
@@ -139,7 +140,7 @@ PdPlan pd_stream_plan(const Dims& d) {
     PdPlan T;
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
-        static const int resident = resident_ctas(k_pd_stream<true>, NT);
+        static const int resident = resident_ctas(k_pd_stream<true, false, int>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
         T.zchunk = wave_zchunk(tiles, d.nz, resident, 1, ZCHUNK);
     } else {
@@ -152,10 +153,15 @@ PdPlan pd_stream_plan(const Dims& d) {
 
 int pd_stream_step(const PdPlan& T, const PdStreamArgs& a, const Dims& d, const StopCtl* ctl, double2* partials,
                    cudaStream_t s) {
-    if (d.nz > 1)
-        k_pd_stream<true><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+    const bool three = d.nz > 1, check = a.check != 0;
+    decltype(&k_pd_stream<true, true, int>) kern;
+    if (d.n < (1LL << 31))
+        kern = three ? (check ? k_pd_stream<true, true, int> : k_pd_stream<true, false, int>)
+                     : (check ? k_pd_stream<false, true, int> : k_pd_stream<false, false, int>);
     else
-        k_pd_stream<false><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+        kern = three ? (check ? k_pd_stream<true, true, long long> : k_pd_stream<true, false, long long>)
+                     : (check ? k_pd_stream<false, true, long long> : k_pd_stream<false, false, long long>);
+    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }
