@@ -24,6 +24,8 @@
 // (the loop is unrolled by two).  The z chunk length balances the CTAs over
 // the SMs (wave_zchunk).  HBM traffic: read U and f, write U
 // (12 B/voxel) plus the tile halo from L2.
+#include <stdlib.h>
+
 #include <type_traits>
 
 #include "rof_tiled.cuh"
@@ -195,6 +197,132 @@ __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ 
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
+// cp.async (sm_80+ asynchronous global -> shared copies, 4 bytes per thread)
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// The 3D iteration with U staged through shared memory by asynchronous copies
+// issued AHEAD planes early into an 8-plane ring, so that load latency is not
+// bound to registers: step j issues plane j+AHEAD, waits for its own copy of
+// plane j, and one barrier makes plane j (and the fluxes of plane j-2) visible
+// to the CTA; then it forms the fluxes of plane j-1 and updates plane j-2 as
+// k_rof_stream does.  Same arithmetic, same tile.
+constexpr int AHEAD = 4;
+constexpr int RING = 8;
+
+template <bool CHECK, bool LARR, typename IT>
+__global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U, float* __restrict__ Un,
+                                                     const float* __restrict__ F, const float* __restrict__ lam_arr,
+                                                     float lam, float tau, Dims d, int zc, const StopCtl* ctl,
+                                                     double2* partials) {
+    __shared__ float sU[RING][BY * BX];
+    __shared__ float sD1[2][BY * BX];
+    __shared__ float sD2[2][BY * BX];
+    if (ctl->stop) return;
+    const float EPS = 1.0e-8f;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny, nz = d.nz;
+    const int x = blockIdx.x * OX + tx - 1;
+    const int y = blockIdx.y * OY + ty - 1;
+    const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
+    const bool o_pt = in_xy && tx >= 1 && tx <= BX - 2 && ty >= 1 && ty <= BY - 2;
+    int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
+    int xl = (nx == 1) ? tx : ((x - 1 < 0) ? tx + 1 : tx - 1);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    xh = min(max(xh, 0), BX - 1);
+    xl = min(max(xl, 0), BX - 1);
+    yh = min(max(yh, 0), BY - 1);
+    yl = min(max(yl, 0), BY - 1);
+    const int oc = ty * BX + tx;
+    const int oxh = ty * BX + xh, oxl = ty * BX + xl, oyh = yh * BX + tx, oyl = yl * BX + tx;
+    const IT col = (IT)min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, nz);
+    const IT sxy = (IT)d.sxy;
+    auto at = [&](int k) -> IT { return (IT)min(max(k, 0), nz - 1) * sxy + col; };
+    auto slot = [&](int k) -> float* { return sU[(k - z0 + 2) & (RING - 1)]; };
+    auto ld_f = [&](int k, float& fv, float& lv) {
+        const IT o = at(k);
+        fv = o_pt ? __ldg(F + o) : 0.f;
+        lv = (LARR && o_pt) ? __ldg(lam_arr + o) : lam;
+    };
+    float pa = 0.f, pb = 0.f;
+    // planes z0-2 .. z0+AHEAD-1 in flight, one copy group per plane
+    for (int k = z0 - 2; k < z0 + AHEAD; k++) {
+        cp_async4(slot(k) + oc, U + at(k));
+        cp_async_commit();
+    }
+    float fa = 0.f, la = lam, fb = 0.f, lb = lam;
+    float d1o = 0.f, d2o = 0.f, d3o = 0.f, d3oo = 0.f;
+
+    auto step = [&](auto par, auto full, int j) {
+        constexpr int P = decltype(par)::value;       // flux ring slot of plane j
+        constexpr bool FULL = decltype(full)::value;  // plane j-2 is updated
+        cp_async4(slot(j + AHEAD) + oc, U + at(j + AHEAD));
+        cp_async_commit();
+        float fe, le;
+        ld_f(j, fe, le);
+        cp_async_wait<AHEAD>();  // this thread's copy of plane j has landed
+        __syncthreads();         // ... and every thread's, and the fluxes of plane j-2
+        const float* Uj = slot(j);
+        const float* Um = slot(j - 1);
+        const float* Ua = slot(j - 2);
+        const float ub = Um[oc], uc = Uj[oc], ua = Ua[oc];
+        // A. fluxes of plane m = j-1
+        const int m = j - 1;
+        const float zlo = (m == 0) ? uc : ua;
+        const float zhi = (m == nz - 1) ? ua : uc;
+        const float xp = Um[oxh] - ub, xm = ub - Um[oxl];
+        const float yp = Um[oyh] - ub, ym = ub - Um[oyl];
+        const float zp = zhi - ub, zm = ub - zlo;
+        const float mx2 = minmod_sq(xp, xm), my2 = minmod_sq(yp, ym), mz2 = minmod_sq(zp, zm);
+        const float n1 = normalise(yp, yp * yp + mx2 + mz2 + EPS);
+        const float n2 = normalise(xp, xp * xp + my2 + mz2 + EPS);
+        const float n3 = normalise(zp, zp * zp + my2 + mx2 + EPS);
+        sD1[1 - P][oc] = n1;
+        sD2[1 - P][oc] = n2;
+        // C. update plane j-2
+        if (FULL) {
+            const int kf = j - 2;
+            const float d3lo = (kf == 0) ? n3 : d3oo;
+            const float div = (d1o - sD1[P][oyl]) + (d2o - sD2[P][oxl]) + (d3o - d3lo);
+            const float un = ua + tau * (la * div - (ua - fa));
+            if (o_pt) Un[(IT)kf * sxy + col] = un;
+            if (CHECK && o_pt) {
+                const float df = un - ua;
+                pa += df * df;
+                pb += un * un;
+            }
+        }
+        fa = fb;
+        la = lb;
+        fb = fe;
+        lb = le;
+        d3oo = d3o;
+        d1o = n1;
+        d2o = n2;
+        d3o = n3;
+    };
+    step(Ic<0>{}, std::false_type{}, z0);
+    step(Ic<1>{}, std::false_type{}, z0 + 1);
+    int j = z0 + 2;
+    for (; j + 1 <= z1 + 1; j += 2) {
+        step(Ic<0>{}, std::true_type{}, j);
+        step(Ic<1>{}, std::true_type{}, j + 1);
+    }
+    if (j <= z1 + 1) step(Ic<0>{}, std::true_type{}, j);
+    cp_async_wait<0>();
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+}
+
 }  // namespace
 
 RofPlan rof_tiled_plan(const Dims& d) {
@@ -216,6 +344,15 @@ RofPlan rof_tiled_plan(const Dims& d) {
 int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,
                    float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
     const bool three = d.nz > 1, larr = lam_arr != nullptr;
+    const char* ek = getenv("CILREG_ROF_KERNEL");
+    if (three && d.n < (1LL << 31) && !(ek && ek[0] == 'r')) {
+        // CILREG_ROF_KERNEL=reg keeps the register-pipelined kernel (A/B checks)
+        auto ka = check ? (larr ? k_rof_async<true, true, int> : k_rof_async<true, false, int>)
+                        : (larr ? k_rof_async<false, true, int> : k_rof_async<false, false, int>);
+        ka<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials);
+        CILREG_CUDA(cudaGetLastError());
+        return OK;
+    }
     decltype(&k_rof_stream<true, true, true, int>) kern;
     if (d.n < (1LL << 31)) {
         kern = three ? (check ? (larr ? k_rof_stream<true, true, true, int> : k_rof_stream<true, true, false, int>)

@@ -225,13 +225,20 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
     rng = np.random.default_rng(11 + sum(shape))
     x = rng.random(shape).astype(np.float32)
     for epsil in (0.0, 1e-3):
-        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
-        a = ROF_TV(x, 0.02, 120, 0.001, epsil, device="gpu", infovector=ia)
+        ib = np.zeros(2, np.float32)
         monkeypatch.setenv("CILREG_ROF_KERNEL", "simple")
         b = ROF_TV(x, 0.02, 120, 0.001, epsil, device="gpu", infovector=ib)
+        # default (3D: asynchronous-copy staging) and the register-pipelined kernel
+        for kernel in (None, "reg"):
+            if kernel is None:
+                monkeypatch.delenv("CILREG_ROF_KERNEL")
+            else:
+                monkeypatch.setenv("CILREG_ROF_KERNEL", kernel)
+            ia = np.zeros(2, np.float32)
+            a = ROF_TV(x, 0.02, 120, 0.001, epsil, device="gpu", infovector=ia)
+            assert int(ia[0]) == int(ib[0])
+            assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
         monkeypatch.delenv("CILREG_ROF_KERNEL")
-        assert int(ia[0]) == int(ib[0])
-        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
