@@ -4,8 +4,9 @@
 //   k_tgv_dual    P += sigma (grad U - V), |P| <= alpha1;
 //                 Q += sigma sym-grad V,   |Q|_F <= alpha0   (reads U, V at +1)
 //   k_tgv_primal  U <- 2 prox(U + tau div P) - U;  V <- 2 (V + tau (P + div Q)) - V
-//                 (reads P, Q at -1); a single volume runs the 2.5D streaming
-//                 version of it (tgv_tiled.cu) unless CILREG_TGV_KERNEL=simple
+//                 (reads P, Q at -1)
+// Volumes below 2^31 voxels run 2.5D streaming versions of both (tgv_tiled.cu)
+// unless CILREG_TGV_KERNEL=simple.
 // 3D state: U, P(3), Q(6), V(3) plus U0.  The dual and primal halves of the
 // reference's ten sweeps (TGV_core.c:136-167) collapse into these two.
 #include "drivers.cuh"
@@ -299,11 +300,14 @@ __global__ void __launch_bounds__(256, 4) k_tgv_primal_batch(const TgvBatchVol* 
 int tgv_batch_step(const TgvBatchVol* d_vols, const int* d_tile_vol, long long ntiles, const int* d_ptile_vol,
                    long long nptiles, bool three, int check, cudaStream_t s) {
     if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    if (d_ptile_vol) {
+        CILREG_TRY(tgv_dual_batch_step(d_vols, d_ptile_vol, nptiles, three, s));
+        return tgv_primal_batch_step(d_vols, d_ptile_vol, nptiles, three, check, s);
+    }
     const dim3 grid((unsigned)ntiles), block(32, 8, 1);
     if (three) k_tgv_dual_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
     else k_tgv_dual_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol);
     CILREG_CUDA(cudaGetLastError());
-    if (d_ptile_vol) return tgv_primal_batch_step(d_vols, d_ptile_vol, nptiles, three, check, s);
     if (three) k_tgv_primal_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
     else k_tgv_primal_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, check);
     CILREG_CUDA(cudaGetLastError());
@@ -348,12 +352,13 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         a.check = check;
-        if (three) k_tgv_dual<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-        else k_tgv_dual<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-        CILREG_CUDA(cudaGetLastError());
         if (T.use) {
+            CILREG_TRY(tgv_dual_stream_step(T, a, d, ctl.ctl(), s));
             CILREG_TRY(tgv_primal_stream_step(T, a, d, ctl.ctl(), ctl.partials(), s));
         } else {
+            if (three) k_tgv_dual<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+            else k_tgv_dual<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
+            CILREG_CUDA(cudaGetLastError());
             if (three) k_tgv_primal<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
             else k_tgv_primal<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl(), ctl.partials());
             CILREG_CUDA(cudaGetLastError());

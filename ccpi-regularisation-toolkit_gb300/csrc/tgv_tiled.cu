@@ -212,6 +212,209 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a1, Dims d1
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, slot);
 }
 
+// The dual half-iteration (DualP + ProjP, DualQ + ProjQ; TGV_core.c:200-275
+// in 2D, 351-446 in 3D) as a 2.5D streaming kernel.  Forward differences of U
+// and V with "0 at the last index": a tile needs a halo of one voxel on its
+// high x and y sides only (thread (tx, ty) on voxel (x0 + tx, y0 + ty), 31 x
+// 15 voxels updated per CTA).  U and V of every thread go to shared memory for
+// the x/y successors; the z successor is the next plane, which each thread
+// holds in registers anyway (loaded one plane ahead).  P and Q are updated in
+// place (each voxel reads only its own).  HBM traffic: read U, V, P, Q; write
+// P, Q (88 B per voxel in 3D, 48 B in 2D).
+template <bool THREE, bool BATCH>
+__global__ void __launch_bounds__(NT, 2) k_tgv_dual_stream(TgvArgs a1, Dims d1, int zc1, const StopCtl* ctl1,
+                                                           const TgvBatchVol* __restrict__ vols,
+                                                           const int* __restrict__ tile_vol) {
+    constexpr int NV = THREE ? 4 : 3;  // U, V1, V2 (, V3)
+    __shared__ float sm[2][NV][BY * BX];
+    __shared__ float* volatile tab[14];
+    __shared__ float sc[3];
+    __shared__ float sa[2];  // alpha1, alpha0
+    int bx, by, bz, zc;
+    Dims d;
+    const StopCtl* ctl;
+    if constexpr (BATCH) {
+        const long long t = blockIdx.x;
+        const TgvBatchVol& V = vols[tile_vol[t]];
+        const long long lt = t - V.ptile_base;
+        bx = (int)(lt % V.pgx);
+        by = (int)((lt / V.pgx) % V.pgy);
+        bz = (int)(lt / ((long long)V.pgx * V.pgy));
+        d = V.d;
+        zc = V.pzc;
+        ctl = V.ctl;
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            publish_args(V.args, tab, sc);
+            sa[0] = V.args.alpha1;
+            sa[1] = V.args.alpha0;
+        }
+    } else {
+        bx = blockIdx.x;
+        by = blockIdx.y;
+        bz = blockIdx.z;
+        d = d1;
+        zc = zc1;
+        ctl = ctl1;
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            publish_args(a1, tab, sc);
+            sa[0] = a1.alpha1;
+            sa[1] = a1.alpha0;
+        }
+    }
+    if (ctl->stop) return;
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny, nz = d.nz;
+    const int x = bx * OX + tx;
+    const int y = by * OY + ty;
+    const bool in_xy = (x < nx) && (y < ny);
+    const bool o_pt = in_xy && tx < OX && ty < OY;
+    const bool xe = (x == nx - 1), ye = (y == ny - 1);
+    const int oc = ty * BX + tx;
+    const int ox = ty * BX + min(tx + 1, BX - 1), oy = min(ty + 1, BY - 1) * BX + tx;
+    const int col = min(y, ny - 1) * nx + min(x, nx - 1);
+    const float sigma = sc[0];  // sigma == tau (TGV_core.c:54-55)
+    const float alpha1 = sa[0], alpha0 = sa[1];
+
+    if constexpr (!THREE) {
+        const float u = __ldg(tab[12] + col), v1 = __ldg(tab[9] + col), v2 = __ldg(tab[10] + col);
+        sm[0][0][oc] = u;
+        sm[0][1][oc] = v1;
+        sm[0][2][oc] = v2;
+        __syncthreads();
+        if (o_pt) {
+            // DualP_2D + ProjP_2D (TGV_core.c:200-232)
+            float p1 = tab[0][col] + (xe ? sigma * (-v1) : sigma * ((sm[0][0][ox] - u) - v1));
+            float p2 = tab[1][col] + (ye ? sigma * (-v2) : sigma * ((sm[0][0][oy] - u) - v2));
+            const float gp = sqrtf(p1 * p1 + p2 * p2) / alpha1;
+            if (gp > 1.0f) {
+                const float ig = __frcp_rn(gp);
+                p1 *= ig;
+                p2 *= ig;
+            }
+            tab[0][col] = p1;
+            tab[1][col] = p2;
+            // DualQ_2D + ProjQ_2D (TGV_core.c:234-275)
+            float q1 = 0.f, q11 = 0.f, q2 = 0.f, q22 = 0.f;
+            if (!xe) {
+                q1 = sm[0][1][ox] - v1;
+                q11 = sm[0][2][ox] - v2;
+            }
+            if (!ye) {
+                q2 = sm[0][2][oy] - v2;
+                q22 = sm[0][1][oy] - v1;
+            }
+            float Q1 = tab[3][col] + sigma * q1;
+            float Q2 = tab[4][col] + sigma * q2;
+            float Q3 = tab[5][col] + sigma * (0.5f * (q11 + q22));
+            float g = sqrtf(Q1 * Q1 + Q2 * Q2 + 2.0f * Q3 * Q3);
+            g = g / alpha0;
+            if (g > 1.0f) {
+                const float ig = __frcp_rn(g);
+                Q1 *= ig;
+                Q2 *= ig;
+                Q3 *= ig;
+            }
+            tab[3][col] = Q1;
+            tab[4][col] = Q2;
+            tab[5][col] = Q3;
+        }
+    } else {
+        const int z0 = bz * zc;
+        const int z1 = min(z0 + zc, nz);
+        const int sxy = (int)d.sxy;
+        auto at = [&](int k) -> int { return min(max(k, 0), nz - 1) * sxy + col; };
+        auto ld_uv = [&](int k, float* w) {
+            const int o = at(k);
+            w[0] = __ldg(tab[12] + o);
+            for (int i = 0; i < 3; i++) w[1 + i] = __ldg(tab[9 + i] + o);
+        };
+        float cw[4], nw[4];  // U, V1..V3 of planes k and k+1
+        ld_uv(z0, cw);
+        ld_uv(z0 + 1, nw);
+
+        auto step = [&](auto par, int k) {
+            constexpr int S = decltype(par)::value;
+            float fw[4];  // plane k+2, used two steps on
+            ld_uv(k + 2, fw);
+            float pq[9];
+            const int o = k * sxy + col;
+            if (o_pt)
+                for (int i = 0; i < 9; i++) pq[i] = tab[i][o];
+            for (int i = 0; i < 4; i++) sm[S][i][oc] = cw[i];
+            __syncthreads();
+            if (o_pt) {
+                const bool ze = (k == nz - 1);
+                const float u = cw[0], v1 = cw[1], v2 = cw[2], v3 = cw[3];
+                // DualP_3D + ProjP_3D (TGV_core.c:351-387)
+                float p1 = pq[0] + (xe ? sigma * (-v1) : sigma * ((sm[S][0][ox] - u) - v1));
+                float p2 = pq[1] + (ye ? sigma * (-v2) : sigma * ((sm[S][0][oy] - u) - v2));
+                float p3 = pq[2] + (ze ? sigma * (-v3) : sigma * ((nw[0] - u) - v3));
+                const float gp = sqrtf(p1 * p1 + p2 * p2 + p3 * p3) / alpha1;
+                if (gp > 1.0f) {
+                    const float ig = __frcp_rn(gp);
+                    p1 *= ig;
+                    p2 *= ig;
+                    p3 *= ig;
+                }
+                tab[0][o] = p1;
+                tab[1][o] = p2;
+                tab[2][o] = p3;
+                // DualQ_3D + ProjQ_3D (TGV_core.c:389-446)
+                float q1 = 0.f, q11 = 0.f, q33 = 0.f, q2 = 0.f, q22 = 0.f, q55 = 0.f, q3 = 0.f, q44 = 0.f, q66 = 0.f;
+                if (!xe) {
+                    q1 = sm[S][1][ox] - v1;
+                    q11 = sm[S][2][ox] - v2;
+                    q33 = sm[S][3][ox] - v3;
+                }
+                if (!ye) {
+                    q2 = sm[S][2][oy] - v2;
+                    q22 = sm[S][1][oy] - v1;
+                    q55 = sm[S][3][oy] - v3;
+                }
+                if (!ze) {
+                    q3 = nw[3] - v3;
+                    q44 = nw[1] - v1;
+                    q66 = nw[2] - v2;
+                }
+                float Q1 = pq[3] + sigma * q1;
+                float Q2 = pq[4] + sigma * q2;
+                float Q3 = pq[5] + sigma * q3;
+                float Q4 = pq[6] + sigma * (0.5f * (q11 + q22));
+                float Q5 = pq[7] + sigma * (0.5f * (q33 + q44));
+                float Q6 = pq[8] + sigma * (0.5f * (q55 + q66));
+                float g = sqrtf(Q1 * Q1 + Q2 * Q2 + Q3 * Q3 + 2.0f * Q4 * Q4 + 2.0f * Q5 * Q5 + 2.0f * Q6 * Q6);
+                g = g / alpha0;
+                if (g > 1.0f) {
+                    const float ig = __frcp_rn(g);
+                    Q1 *= ig;
+                    Q2 *= ig;
+                    Q3 *= ig;
+                    Q4 *= ig;
+                    Q5 *= ig;
+                    Q6 *= ig;
+                }
+                tab[3][o] = Q1;
+                tab[4][o] = Q2;
+                tab[5][o] = Q3;
+                tab[6][o] = Q4;
+                tab[7][o] = Q5;
+                tab[8][o] = Q6;
+            }
+            for (int i = 0; i < 4; i++) {
+                cw[i] = nw[i];
+                nw[i] = fw[i];
+            }
+        };
+        int k = z0;
+        for (; k + 1 < z1; k += 2) {
+            step(Ic<0>{}, k);
+            step(Ic<1>{}, k + 1);
+        }
+        if (k < z1) step(Ic<0>{}, k);
+    }
+}
+
 }  // namespace
 
 TgvPlan tgv_primal_plan(const Dims& d) {
@@ -239,6 +442,23 @@ int tgv_primal_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, co
     auto kern = three ? (a.check ? k_tgv_primal_stream<true, true, false> : k_tgv_primal_stream<true, false, false>)
                       : (a.check ? k_tgv_primal_stream<false, true, false> : k_tgv_primal_stream<false, false, false>);
     kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials, nullptr, nullptr);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int tgv_dual_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, cudaStream_t s) {
+    auto kern = (d.nz > 1) ? k_tgv_dual_stream<true, false> : k_tgv_dual_stream<false, false>;
+    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, nullptr, nullptr);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int tgv_dual_batch_step(const TgvBatchVol* d_vols, const int* d_ptile_vol, long long nptiles, bool three,
+                        cudaStream_t s) {
+    if (nptiles < 1 || nptiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", nptiles);
+    auto kern = three ? k_tgv_dual_stream<true, true> : k_tgv_dual_stream<false, true>;
+    TgvArgs none{};
+    kern<<<dim3((unsigned)nptiles), dim3(BX, BY, 1), 0, s>>>(none, Dims{}, 1, nullptr, d_vols, d_ptile_vol);
     CILREG_CUDA(cudaGetLastError());
     return OK;
 }

@@ -1,4 +1,4 @@
-// TGV primal half-iteration as a 2.5D streaming kernel (tgv_tiled.cu).
+// TGV dual and primal half-iterations as 2.5D streaming kernels (tgv_tiled.cu).
 #pragma once
 
 #include "tgv_batch.cuh"
@@ -9,12 +9,18 @@ struct TgvPlan {
     dim3 grid, block;
     long long nblocks = 0;
     int zchunk = 0;
-    bool use = false;  // false: the per-voxel primal kernel of tgv.cu runs instead
+    bool use = false;  // false: the per-voxel kernels of tgv.cu run instead
 };
 
 TgvPlan tgv_primal_plan(const Dims& d);
 int tgv_primal_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, double2* partials,
                            cudaStream_t s);
+
+// the dual half-iteration as a streaming kernel on the same tiling (forward
+// differences: a one-voxel halo on the high x/y sides), single volume / batch
+int tgv_dual_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, const StopCtl* ctl, cudaStream_t s);
+int tgv_dual_batch_step(const TgvBatchVol* d_vols, const int* d_ptile_vol, long long nptiles, bool three,
+                        cudaStream_t s);
 
 // tiling of the streaming primal kernel in a batched run (64-plane chunks)
 void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);

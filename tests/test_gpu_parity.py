@@ -284,9 +284,9 @@ def test_sb_fused_sweeps_equal_per_sweep_kernels(shape, monkeypatch):
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
                                    (130, 33, 35)], ids=str)
-def test_tgv_streaming_primal_equals_per_voxel_kernel(shape, monkeypatch):
-    """The 2.5D streaming TGV primal kernel and the per-voxel one compute the
-    same iteration (and the same stopping iteration)."""
+def test_tgv_streaming_kernels_equal_per_voxel_kernels(shape, monkeypatch):
+    """The 2.5D streaming TGV dual and primal kernels and the per-voxel ones
+    compute the same iteration (and the same stopping iteration)."""
     from ccpi.filters.regularisers import TGV
 
     rng = np.random.default_rng(31 + sum(shape))
