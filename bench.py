@@ -420,6 +420,79 @@ def serve_bench(args):
     return 0
 
 
+def configs_bench(args):
+    """Configs C1 (ROF 2D 512^2, 2000 iterations) and C2 (FGP and PD 3D at
+    256^3 and 512^3, up to 500 iterations, epsil 1e-6) end to end through the
+    reference-compatible Python API with host arrays (device='gpu'; copies
+    included), each beside the reference CPU implementation on the host cores:
+    C1 in full, C2 as a fixed 20-iteration sample (per-iteration cost is
+    constant), projected to the iterations the GPU ran."""
+    from ccpi.filters.regularisers import FGP_TV, PD_TV, ROF_TV
+    from ccpi.supp.phantoms import noisy_phantom
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    use_ref = O.ref_lib() is not None
+    kind, cores = ("reference" if use_ref else "port"), O.num_threads()
+
+    def gpu_time(fn, reps=3):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t = time.perf_counter()
+            info = fn()
+            ts.append(time.perf_counter() - t)
+        return statistics.median(ts), info
+
+    rows = []
+    img = noisy_phantom((512, 512), 10, 0)
+
+    def c1():
+        info = np.zeros(2, np.float32)
+        ROF_TV(img, 0.02, 2000, 0.001, 0.0, device="gpu", infovector=info)
+        return info
+
+    g, info = gpu_time(c1)
+    t = time.perf_counter()
+    O.rof_tv(img, 0.02, 2000, 0.001, 0.0, use_ref=use_ref)
+    c = time.perf_counter() - t
+    rows.append({"config": "C1 ROF_TV 2D 512^2, lambda 0.02, tau 0.001, 2000 iterations", "gpu_s": g,
+                 "gpu_iterations": int(info[0]), "gpu_voxel_iters_per_s": img.size * 2000 / g, "cpu_s": c,
+                 "cpu_sample": "full call", "cpu_kind": kind, "cpu_cores": cores, "speedup": c / g})
+    for size in (256, 512):
+        vol = noisy_phantom((size,) * 3, 30, 1)
+        for name in ("FGP_TV", "PD_TV"):
+            def call():
+                info = np.zeros(2, np.float32)
+                if name == "FGP_TV":
+                    FGP_TV(vol, 0.03, 500, 1e-6, 0, 1, device="gpu", infovector=info)
+                else:
+                    PD_TV(vol, 0.03, 500, 1e-6, 8.0, 0, 1, device="gpu", infovector=info)
+                return info
+
+            g, info = gpu_time(call, reps=2)
+            its = int(info[0])
+            t = time.perf_counter()
+            if name == "FGP_TV":
+                O.fgp_tv(vol, 0.03, 20, 0.0, 0, 1, use_ref=use_ref)
+            else:
+                O.pd_tv(vol, 0.03, 20, 0.0, 8.0, 0, 1, use_ref=use_ref)
+            c20 = time.perf_counter() - t
+            cpu_rate = vol.size * 20 / c20
+            c = vol.size * max(its, 1) / cpu_rate
+            rows.append({"config": f"C2 {name} 3D {size}^3, lambda 0.03, up to 500 iterations, epsil 1e-6, iso, nonneg",
+                         "gpu_s": g, "gpu_iterations": its, "gpu_voxel_iters_per_s": vol.size * its / g,
+                         "cpu_s": c, "cpu_sample": f"20 fixed iterations ({c20:.1f} s), projected to {its}",
+                         "cpu_kind": kind, "cpu_cores": cores, "cpu_voxel_iters_per_s": cpu_rate,
+                         "speedup": c / g})
+    for r in rows:
+        print(json.dumps(r))
+    print(json.dumps({"configs": rows}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -441,6 +514,8 @@ def main():
     ap.add_argument("--serve", action="store_true",
                     help="Poisson stream (mean 200 req/s) of prox requests through the continuous-batching server")
     ap.add_argument("--requests", type=int, default=48, help="requests of the --serve stream")
+    ap.add_argument("--configs", action="store_true",
+                    help="configs C1 and C2 through the Python API (host arrays) beside the reference CPU")
     ap.add_argument("--regs", default="", help="comma-separated regularisers of --suite (default: all)")
     ap.add_argument("--suite", action="store_true",
                     help="per-regulariser iteration time and roofline fraction (device data, fixed counts)")
@@ -453,6 +528,8 @@ def main():
         return profile_case(args)
     if args.suite:
         return suite(args)
+    if args.configs:
+        return configs_bench(args)
     if args.batch:
         return batch_bench(args)
     if args.autograd:
