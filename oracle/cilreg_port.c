@@ -2,7 +2,8 @@
  * ORACLE — TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C, CPU restatement of the seven iterative proximal regularisers of
- * the CCPi Regularisation Toolkit (C-OMP path, FP32).  It exists so that the
+ * the CCPi Regularisation Toolkit (C-OMP path, FP32), of LLT-ROF and FGP-dTV
+ * and of the TV energy diagnostic.  It exists so that the
  * GPU product can be checked against the reference's arithmetic on the GPU
  * machine, where the reference sources are not available.  Only the test
  * suite, the smoke check and the CPU-baseline leg of the benchmark load it;
@@ -101,7 +102,9 @@ static inline float rof_minmod(float a, float b)
     return (float)(0.5f * (sgn_f(a) + sgn_f(b)) * fmin(fabs(a), fabs(b)));
 }
 
-static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx, idx_t ny, idx_t nz)
+/* eps: 1e-8 for ROF-TV (ROF_TV_core.c:22), 1e-12 inside LLT-ROF (LLT_ROF_core.c:22) */
+static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx, idx_t ny, idx_t nz,
+                       double eps)
 {
     idx_t i, j, k;
     if (nz > 1) {
@@ -123,7 +126,7 @@ static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx
                         float d1 = dyp * dyp, d2, d3;
                         m = rof_minmod(dxp, dxm); d2 = m * m;
                         m = rof_minmod(dzp, dzm); d3 = m * m;
-                        t1 = (float)sqrt(d1 + d2 + d3 + 1.0e-8);
+                        t1 = (float)sqrt(d1 + d2 + d3 + eps);
                         D1[v] = dyp / t1;
                     }
                     /* D2 (i axis): ROF_TV_core.c:194-200 */
@@ -131,7 +134,7 @@ static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx
                         float d1 = dxp * dxp, d2, d3;
                         m = rof_minmod(dyp, dym); d2 = m * m;
                         m = rof_minmod(dzp, dzm); d3 = m * m;
-                        t2 = sqrtf((float)(d1 + d2 + d3 + 1.0e-8));
+                        t2 = sqrtf((float)(d1 + d2 + d3 + eps));
                         D2[v] = dxp / t2;
                     }
                     /* D3 (k axis): ROF_TV_core.c:257-263 */
@@ -139,7 +142,7 @@ static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx
                         float d1 = dzp * dzp, d2, d3;
                         m = rof_minmod(dyp, dym); d2 = m * m;
                         m = rof_minmod(dxp, dxm); d3 = m * m;
-                        t3 = sqrtf((float)(d1 + d2 + d3 + 1.0e-8));
+                        t3 = sqrtf((float)(d1 + d2 + d3 + eps));
                         D3[v] = dzp / t3;
                     }
                 }
@@ -155,9 +158,9 @@ static void rof_fluxes(const float *A, float *D1, float *D2, float *D3, idx_t nx
                 float dxp = A[nx * j + ip] - a, dxm = a - A[nx * j + im];
                 float m, d1, d2;
                 d1 = dyp * dyp; m = rof_minmod(dxp, dxm); d2 = m * m;
-                D1[v] = dyp / sqrtf((float)(d1 + d2 + 1.0e-8));
+                D1[v] = dyp / sqrtf((float)(d1 + d2 + eps));
                 d1 = dxp * dxp; m = rof_minmod(dyp, dym); d2 = m * m;
-                D2[v] = dxp / sqrtf((float)(d1 + d2 + 1.0e-8));
+                D2[v] = dxp / sqrtf((float)(d1 + d2 + eps));
             }
     }
 }
@@ -204,7 +207,7 @@ float port_TV_ROF(float *Input, float *Output, float *infovector, float *lambdaP
     for (it = 0; it < iterationsNumb; it++) {
         int check = (epsil != 0.0f) && (it % 5 == 0);
         if (check) copy_arr(Output, Uprev, n);
-        rof_fluxes(Output, D1, D2, D3, nx, ny, nz);
+        rof_fluxes(Output, D1, D2, D3, nx, ny, nz, 1.0e-8);
         rof_update(D1, D2, D3, Output, Input, lambdaPar, lambda_is_arr, tau, nx, ny, nz);
         if (check && stop_check(&st, Output, Uprev, n, epsil)) break;
     }
@@ -827,4 +830,231 @@ int port_num_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------ */
+/* LLT-ROF: fourth-order LLT + ROF-TV explicit flow                     */
+/* (LLT_ROF_core.c:54-436)                                             */
+/* ------------------------------------------------------------------ */
+float port_LLT_ROF(float *Input, float *Output, float *infovector, float lambdaROF, float lambdaLLT,
+                   int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ)
+{
+    if (dimZ < 1) dimZ = 1;
+    idx_t nx = dimX, ny = dimY, nz = dimZ, n = nx * ny * nz, s = nx * ny;
+    int three = nz > 1, it;
+    float *R1 = zalloc(n), *R2 = zalloc(n), *R3 = zalloc(n);  /* ROF fluxes */
+    float *L1 = zalloc(n), *L2 = zalloc(n), *L3 = zalloc(n);  /* normalised second derivatives */
+    float *Uprev = NULL;
+    stop_state st = {0.0f, 0};
+    copy_arr(Input, Output, n);
+    if (epsil != 0.0f) Uprev = zalloc(n);
+    for (it = 0; it < iterationsNumb; it++) {
+        int check = (epsil != 0.0f) && (it % 5 == 0);
+        idx_t i, j, k;
+        if (check) copy_arr(Output, Uprev, n);
+        rof_fluxes(Output, R1, R2, R3, nx, ny, nz, 1.0e-12);
+        /* der2D_LLT / der3D_LLT (LLT_ROF_core.c:131-188): dxx / (|dxx| + 1e-12) */
+#pragma omp parallel for private(i, j)
+        for (k = 0; k < nz; k++)
+            for (j = 0; j < ny; j++)
+                for (i = 0; i < nx; i++) {
+                    idx_t v = s * k + nx * j + i;
+                    float u = Output[v];
+                    float dxx = Output[s * k + nx * j + nb_hi(i, nx)] - 2.0f * u + Output[s * k + nx * j + nb_lo(i, nx)];
+                    float dyy = Output[s * k + nx * nb_hi(j, ny) + i] - 2.0f * u + Output[s * k + nx * nb_lo(j, ny) + i];
+                    L1[v] = (float)(dxx / (fabs(dxx) + 1.0e-12));
+                    L2[v] = (float)(dyy / (fabs(dyy) + 1.0e-12));
+                    if (three) {
+                        float dzz = Output[s * nb_hi(k, nz) + nx * j + i] - 2.0f * u + Output[s * nb_lo(k, nz) + nx * j + i];
+                        L3[v] = (float)(dzz / (fabs(dzz) + 1.0e-12));
+                    }
+                }
+        /* Update2D_LLT_ROF / Update3D_LLT_ROF (LLT_ROF_core.c:377-436) */
+#pragma omp parallel for private(i, j)
+        for (k = 0; k < nz; k++)
+            for (j = 0; j < ny; j++)
+                for (i = 0; i < nx; i++) {
+                    idx_t v = s * k + nx * j + i;
+                    idx_t ip = nb_hi(i, nx), im = nb_lo(i, nx), jp = nb_hi(j, ny), jm = nb_lo(j, ny);
+                    float dxx = L1[s * k + nx * j + ip] - 2.0f * L1[v] + L1[s * k + nx * j + im];
+                    float dyy = L2[s * k + nx * jp + i] - 2.0f * L2[v] + L2[s * k + nx * jm + i];
+                    float laplc, div;
+                    if (three) {
+                        idx_t kp = nb_hi(k, nz), km = nb_lo(k, nz);
+                        float dzz = L3[s * kp + nx * j + i] - 2.0f * L3[v] + L3[s * km + nx * j + i];
+                        laplc = dxx + dyy + dzz;
+                        div = (R1[v] - R1[s * k + nx * jm + i]) + (R2[v] - R2[s * k + nx * j + im]) +
+                              (R3[v] - R3[s * km + nx * j + i]);
+                    } else {
+                        laplc = dxx + dyy;
+                        div = (R1[v] - R1[s * k + nx * jm + i]) + (R2[v] - R2[s * k + nx * j + im]);
+                    }
+                    Output[v] += tau * (lambdaROF * div - lambdaLLT * laplc - (Output[v] - Input[v]));
+                }
+        if (check && stop_check(&st, Output, Uprev, n, epsil)) break;
+    }
+    free(R1); free(R2); free(R3); free(L1); free(L2); free(L3); free(Uprev);
+    infovector[0] = (float)it;
+    infovector[1] = st.re;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* FGP-dTV: FGP on the directional TV of a reference image             */
+/* (FGP_dTV_core.c:46-380)                                             */
+/* ------------------------------------------------------------------ */
+float port_dTV_FGP(float *Input, float *InputRef, float *Output, float *infovector, float lambdaPar,
+                   int iterationsNumb, float epsil, float eta, int methodTV, int nonneg, int dimX, int dimY,
+                   int dimZ)
+{
+    if (dimZ < 1) dimZ = 1;
+    int three = dimZ > 1;
+    idx_t nx = dimX, ny = dimY, nz = three ? dimZ : 1, n = nx * ny * nz, s = nx * ny;
+    float *P[3] = {0}, *Pold[3] = {0}, *R[3] = {0}, *B[3] = {0}, *Uprev = NULL;
+    int c, na = three ? 3 : 2, it;
+    float tk = 1.0f, tkp1 = 1.0f;
+    float multip = three ? (1.0f / (26.0f * lambdaPar)) : (1.0f / (8.0f * lambdaPar));
+    float eta_sq = eta * eta;
+    stop_state st = {0.0f, 0};
+    idx_t i, j, k;
+    for (c = 0; c < na; c++) { P[c] = zalloc(n); Pold[c] = zalloc(n); R[c] = zalloc(n); B[c] = zalloc(n); }
+    if (epsil != 0.0f) Uprev = zalloc(n);
+    /* GradNorm_func2D/3D (:187-205, 273-300): eta-smoothed unit gradient of the
+     * reference, forward differences with 0 beyond the last index */
+#pragma omp parallel for private(i, j)
+    for (k = 0; k < nz; k++)
+        for (j = 0; j < ny; j++)
+            for (i = 0; i < nx; i++) {
+                idx_t v = s * k + nx * j + i;
+                float b = InputRef[v];
+                float gx = ((i == nx - 1) ? 0.0f : InputRef[v + 1]) - b;
+                float gy = ((j == ny - 1) ? 0.0f : InputRef[v + nx]) - b;
+                float magn;
+                if (three) {
+                    float gz = ((k == nz - 1) ? 0.0f : InputRef[v + s]) - b;
+                    magn = gx * gx + gy * gy + gz * gz;
+                    magn = (float)sqrt(magn + eta_sq);
+                    B[2][v] = gz / magn;
+                } else {
+                    magn = gx * gx + gy * gy;
+                    magn = (float)sqrt(magn + eta_sq);
+                }
+                B[0][v] = gx / magn;
+                B[1][v] = gy / magn;
+            }
+    for (it = 0; it < iterationsNumb; it++) {
+        int check = (epsil != 0.0f) && (it % 5 == 0);
+        if (check) copy_arr(Output, Uprev, n);
+        /* ProjectVect_func (:207-219, 302-317): R onto the complement of B */
+#pragma omp parallel for
+        for (i = 0; i < n; i++) {
+            if (three) {
+                float ip = R[0][i] * B[0][i] + R[1][i] * B[1][i] + R[2][i] * B[2][i];
+                R[0][i] = R[0][i] - ip * B[0][i];
+                R[1][i] = R[1][i] - ip * B[1][i];
+                R[2][i] = R[2][i] - ip * B[2][i];
+            } else {
+                float ip = R[0][i] * B[0][i] + R[1][i] * B[1][i];
+                R[0][i] = R[0][i] - ip * B[0][i];
+                R[1][i] = R[1][i] - ip * B[1][i];
+            }
+        }
+        /* Obj_dfunc (:221-234, 319-334): U = f - lambda div R, zero below index 0 */
+#pragma omp parallel for private(i, j)
+        for (k = 0; k < nz; k++)
+            for (j = 0; j < ny; j++)
+                for (i = 0; i < nx; i++) {
+                    idx_t v = s * k + nx * j + i;
+                    float b1 = (i == 0) ? 0.0f : R[0][v - 1];
+                    float b2 = (j == 0) ? 0.0f : R[1][v - nx];
+                    if (three) {
+                        float b3 = (k == 0) ? 0.0f : R[2][v - s];
+                        Output[v] = Input[v] - lambdaPar * (R[0][v] + R[1][v] + R[2][v] - b1 - b2 - b3);
+                    } else {
+                        Output[v] = Input[v] - lambdaPar * (R[0][v] + R[1][v] - b1 - b2);
+                    }
+                }
+        if (nonneg == 1) clamp_nonneg(Output, n);
+        /* Grad_dfunc (:235-253, 335-363): gradient projected onto the complement of B */
+#pragma omp parallel for private(i, j)
+        for (k = 0; k < nz; k++)
+            for (j = 0; j < ny; j++)
+                for (i = 0; i < nx; i++) {
+                    idx_t v = s * k + nx * j + i;
+                    float g1 = (i == nx - 1) ? 0.0f : Output[v] - Output[v + 1];
+                    float g2 = (j == ny - 1) ? 0.0f : Output[v] - Output[v + nx];
+                    if (three) {
+                        float g3 = (k == nz - 1) ? 0.0f : Output[v] - Output[v + s];
+                        float ip = g1 * B[0][v] + g2 * B[1][v] + g3 * B[2][v];
+                        g1 = g1 - ip * B[0][v];
+                        g2 = g2 - ip * B[1][v];
+                        g3 = g3 - ip * B[2][v];
+                        P[2][v] = R[2][v] + multip * g3;
+                    } else {
+                        float ip = g1 * B[0][v] + g2 * B[1][v];
+                        g1 = g1 - ip * B[0][v];
+                        g2 = g2 - ip * B[1][v];
+                    }
+                    P[0][v] = R[0][v] + multip * g1;
+                    P[1][v] = R[1][v] + multip * g2;
+                }
+        project_dual(P[0], P[1], three ? P[2] : NULL, methodTV, n);
+        tkp1 = (float)((1.0f + sqrt(1.0f + 4.0f * tk * tk)) * 0.5f);
+        {
+            float m = (tk - 1.0f) / tkp1;
+#pragma omp parallel for
+            for (i = 0; i < n; i++)
+                for (c = 0; c < na; c++) R[c][i] = P[c][i] + m * (P[c][i] - Pold[c][i]);
+        }
+        for (c = 0; c < na; c++) copy_arr(P[c], Pold[c], n);
+        tk = tkp1;
+        if (check && stop_check(&st, Output, Uprev, n, epsil)) break;
+    }
+    for (c = 0; c < na; c++) { free(P[c]); free(Pold[c]); free(R[c]); free(B[c]); }
+    free(Uprev);
+    infovector[0] = (float)it;
+    infovector[1] = st.re;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* TV energy (utils.c:60-117): sequential FP32 sums in the reference's   */
+/* loop order (2D: j, i; 3D: j, i, k)                                    */
+/* ------------------------------------------------------------------ */
+float port_TV_energy2D(float *U, float *U0, float *E_val, float lambda, int type, int dimX, int dimY)
+{
+    idx_t i, j, nx = dimX, ny = dimY;
+    float eg = 0.0f, ed = 0.0f;
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++) {
+            idx_t v = nx * j + i;
+            idx_t i1 = (i == nx - 1) ? i : i + 1, j1 = (j == ny - 1) ? j : j + 1;
+            float a = powf(U[nx * j1 + i] - U[v], 2);
+            float b = powf(U[nx * j + i1] - U[v], 2);
+            eg += 2.0f * lambda * sqrtf(a + b);
+            ed += powf(U[v] - U0[v], 2);
+        }
+    if (type == 1) E_val[0] = eg + ed;
+    if (type == 2) E_val[0] = eg;
+    return E_val[0];
+}
+
+float port_TV_energy3D(float *U, float *U0, float *E_val, float lambda, int type, int dimX, int dimY, int dimZ)
+{
+    idx_t i, j, k, nx = dimX, ny = dimY, nz = dimZ, s = nx * ny;
+    float eg = 0.0f, ed = 0.0f;
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++)
+            for (k = 0; k < nz; k++) {
+                idx_t v = s * k + nx * j + i;
+                idx_t i1 = (i == nx - 1) ? i : i + 1, j1 = (j == ny - 1) ? j : j + 1, k1 = (k == nz - 1) ? k : k + 1;
+                float a = powf(U[s * k + nx * j1 + i] - U[v], 2);
+                float b = powf(U[s * k + nx * j + i1] - U[v], 2);
+                float c = powf(U[s * k1 + nx * j + i] - U[v], 2);
+                eg += 2.0f * lambda * sqrtf(a + b + c);
+                ed += powf(U[v] - U0[v], 2);
+            }
+    if (type == 1) E_val[0] = eg + ed;
+    if (type == 2) E_val[0] = eg;
+    return E_val[0];
 }

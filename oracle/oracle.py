@@ -82,6 +82,7 @@ _SIGS = {
     "TGV": ("TGV_main", "port_TGV", [_F, _F, _F, _I, _F, _F]),
     "Diffusion": ("Diffusion_CPU_main", "port_Diffusion", [_F, _F, _I, _F, _I, _F]),
     "Diffus4th": ("Diffus4th_CPU_main", "port_Diffus4th", [_F, _F, _I, _F, _F]),
+    "LLT_ROF": ("LLT_ROF_CPU_main", "port_LLT_ROF", [_F, _F, _I, _F, _F]),
 }
 
 
@@ -93,6 +94,15 @@ def _declare(lib, prefix):
         if prefix and key == "Diffusion":
             args = args + [_I]  # jacobi flag
         fn.argtypes = args
+        fn.restype = ctypes.c_float
+    # FGP-dTV: (Input, InputRef, Output, infovector, lambda, iters, epsil, eta, methodTV, nonneg, dims)
+    fn = getattr(lib, "port_dTV_FGP" if prefix else "dTV_FGP_CPU_main")
+    fn.argtypes = [_P, _P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I]
+    fn.restype = ctypes.c_float
+    # TV energy: (U, U0, E_val, lambda, type, dims)
+    for nd in (2, 3):
+        fn = getattr(lib, (f"port_TV_energy{nd}D" if prefix else f"TV_energy{nd}D"))
+        fn.argtypes = [_P, _P, _P, _F, _I] + [_I] * nd
         fn.restype = ctypes.c_float
 
 
@@ -190,6 +200,41 @@ def diff4th(x, lam, sigma, iters, tau, epsil, use_ref=False):
     fn = lib.port_Diffus4th if is_port else lib.Diffus4th_CPU_main
     fn(_ptr(a), _ptr(out), _ptr(info), lam, sigma, iters, tau, epsil, *_dims(a))
     return out, info
+
+
+def llt_rof(x, lam_rof, lam_llt, iters, tau, epsil, use_ref=False):
+    """LLT-ROF (LLT_ROF_core.c:54)."""
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    fn = lib.port_LLT_ROF if is_port else lib.LLT_ROF_CPU_main
+    fn(_ptr(a), _ptr(out), _ptr(info), lam_rof, lam_llt, iters, tau, epsil, *_dims(a))
+    return out, info
+
+
+def dtv_fgp(x, ref, lam, iters, epsil, eta, method_tv=0, nonneg=0, use_ref=False):
+    """FGP-dTV (FGP_dTV_core.c:46): `ref` is the reference image of x's shape."""
+    lib, is_port = _lib(use_ref)
+    a, out, info = _prep(x)
+    r = np.ascontiguousarray(ref, dtype=np.float32)
+    assert r.shape == a.shape
+    fn = lib.port_dTV_FGP if is_port else lib.dTV_FGP_CPU_main
+    fn(_ptr(a), _ptr(r), _ptr(out), _ptr(info), lam, iters, epsil, eta, method_tv, nonneg, *_dims(a))
+    return out, info
+
+
+def tv_energy(u, u0, lam, typ, use_ref=False):
+    """TV energy (utils.c:60-117): type 1 = 2 lambda TV(u) + |u - u0|^2, type 2 = 2 lambda TV(u)."""
+    lib, is_port = _lib(use_ref)
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    u0 = np.ascontiguousarray(u0, dtype=np.float32)
+    e = np.zeros(1, np.float32)
+    if u.ndim == 2:
+        fn = lib.port_TV_energy2D if is_port else lib.TV_energy2D
+        fn(_ptr(u), _ptr(u0), _ptr(e), lam, typ, u.shape[1], u.shape[0])
+    else:
+        fn = lib.port_TV_energy3D if is_port else lib.TV_energy3D
+        fn(_ptr(u), _ptr(u0), _ptr(e), lam, typ, u.shape[2], u.shape[1], u.shape[0])
+    return float(e[0])
 
 
 def num_threads() -> int:

@@ -94,3 +94,27 @@ def test_invalid_penalty_rejected_by_port():
     a, out, info = O._prep(x)
     r = lib.port_Diffusion(O._ptr(a), O._ptr(out), O._ptr(info), 0.02, 0.05, 10, 0.01, 9, 0.0, *O._dims(a), 1)
     assert r < 0
+
+
+@pytest.mark.parametrize("shape", [(40, 56), (3, 5), (10, 16, 22), (5, 4, 3), (13, 9, 2)])
+def test_port_matches_live_reference_llt_dtv_energy(shape):
+    """LLT-ROF, FGP-dTV and the TV energy of the port against the reference
+    compiled here (skipped where its sources are absent).  Axes of length 1
+    are left out: there the reference indexes outside the array."""
+    if O.ref_lib() is None:
+        pytest.skip("reference C-OMP library not built on this machine")
+    rng = np.random.default_rng(7 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    ref = rng.random(shape).astype(np.float32)
+    for epsil in (0.0, 1e-3):
+        a, ia = O.llt_rof(x, 0.02, 0.01, 40, 0.002, epsil)
+        b, ib = O.llt_rof(x, 0.02, 0.01, 40, 0.002, epsil, use_ref=True)
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(ia, ib)
+        for method, nonneg in ((0, 1), (1, 0)):
+            a, ia = O.dtv_fgp(x, ref, 0.05, 40, epsil, 0.2, method, nonneg)
+            b, ib = O.dtv_fgp(x, ref, 0.05, 40, epsil, 0.2, method, nonneg, use_ref=True)
+            np.testing.assert_array_equal(a, b)
+            np.testing.assert_array_equal(ia, ib)
+    for typ in (1, 2):
+        assert O.tv_energy(x, ref, 0.1, typ) == O.tv_energy(x, ref, 0.1, typ, use_ref=True)
