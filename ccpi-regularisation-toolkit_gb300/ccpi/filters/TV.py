@@ -1,5 +1,6 @@
 """Total-variation family: same functions and signatures as the reference's
-src/Python/ccpi/filters/TV.py (ROF, FGP, PD, SB, TGV).
+src/Python/ccpi/filters/TV.py (ROF, FGP, PD, SB, TGV, LLT-ROF, FGP-dTV and the
+TV energy diagnostic).
 
 ``*_CPU`` functions call the ``*_CPU_main`` entry points of ``libcilreg.so``,
 which in this build execute on the GPU named by ``CILREG_GPU_DEVICE``
@@ -156,12 +157,86 @@ def _not_provided(name):
     return f
 
 
-LLT_ROF_CPU = _not_provided("LLT_ROF")
-LLT_ROF_GPU = _not_provided("LLT_ROF")
-dTV_FGP_CPU = _not_provided("FGP_dTV")
-dTV_FGP_GPU = _not_provided("FGP_dTV")
 PatchSelect_CPU = _not_provided("PatchSelect")
 PatchSelect_GPU = _not_provided("PatchSelect")
 NLTV = _not_provided("NLTV")
 TNV = _not_provided("TNV")
-TV_ENERGY = _not_provided("TV_ENERGY")
+
+
+# ---------------------------------------------------------------------------
+# LLT-ROF, FGP-dTV and the TV energy (TV.py:174-250, 252-290, 421-459,
+# 650-689, 735-780 of the reference)
+def _as_like(b, a, name):
+    b = as_input(b)
+    if b.shape != a.shape:
+        raise ValueError(f"{name} has shape {b.shape}, expected {a.shape}")
+    return b
+
+
+def LLT_ROF_CPU(inputData, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil, out=None, infovector=None):
+    """LLT-ROF (LLT_ROF_core.c:54): fourth-order LLT plus ROF-TV explicit flow."""
+    a = as_input(inputData)
+    out = as_output(out, a)
+    info = as_info(infovector)
+    st = cilreg.LLT_ROF_CPU_main(ptr(a), ptr(out), ptr(info), float(lambdaROF), float(lambdaLLT),
+                                 int(iterationsNumb), float(tau), float(epsil), *dims(a))
+    check_status(st, cilreg)
+    return out
+
+
+def LLT_ROF_GPU(inputData, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil, gpu_device, out=None,
+                infovector=None):
+    a = as_input(inputData)
+    out = as_output(out, a)
+    info = as_info(infovector)
+    st = cilregcuda.LLT_ROF_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaROF), float(lambdaLLT),
+                                     int(iterationsNumb), float(tau), float(epsil), _dev(gpu_device), *dims(a))
+    check_status(st)
+    return out
+
+
+def dTV_FGP_CPU(inputData, inputRef, lambdaPar, iterationsNumb, epsil, eta, methodTV, nonneg, out=None,
+                infovector=None):
+    """FGP-dTV (FGP_dTV_core.c:46): FGP on the directional TV guided by inputRef."""
+    a = as_input(inputData)
+    r = _as_like(inputRef, a, "inputRef")
+    out = as_output(out, a)
+    info = as_info(infovector)
+    st = cilreg.dTV_FGP_CPU_main(ptr(a), ptr(r), ptr(out), ptr(info), float(lambdaPar), int(iterationsNumb),
+                                 float(epsil), float(eta), int(methodTV), int(nonneg), *dims(a))
+    check_status(st, cilreg)
+    return out
+
+
+def dTV_FGP_GPU(inputData, inputRef, lambdaPar, iterationsNumb, epsil, eta, methodTV, nonneg, gpu_device,
+                out=None, infovector=None):
+    a = as_input(inputData)
+    r = _as_like(inputRef, a, "inputRef")
+    out = as_output(out, a)
+    info = as_info(infovector)
+    st = cilregcuda.dTV_FGP_GPU_main(ptr(a), ptr(r), ptr(out), ptr(info), float(lambdaPar), int(iterationsNumb),
+                                     float(epsil), float(eta), int(methodTV), int(nonneg), _dev(gpu_device),
+                                     *dims(a))
+    check_status(st)
+    return out
+
+
+def TV_ENERGY(U, U0, lambdaPar, type, E_val=None):
+    """TV energy (utils.c:60-117): type 1 gives 2 lambda TV(U) + |U - U0|^2,
+    type 2 gives 2 lambda TV(U).  Returns a float32 array of one element."""
+    u = as_input(U)
+    u0 = _as_like(U0, u, "U0")
+    if E_val is None:
+        E_val = np.zeros((1,), dtype=np.float32)
+    elif not isinstance(E_val, np.ndarray) or E_val.dtype != np.float32 or E_val.size < 1:
+        raise TypeError("E_val must be a float32 ndarray with at least one element")
+    if int(type) not in (1, 2):
+        raise ValueError(f"TV_ENERGY: type must be 1 or 2, got {type}")
+    if u.ndim == 2:
+        r = cilreg.TV_energy2D(ptr(u), ptr(u0), ptr(E_val), float(lambdaPar), int(type), u.shape[1], u.shape[0])
+    else:
+        r = cilreg.TV_energy3D(ptr(u), ptr(u0), ptr(E_val), float(lambdaPar), int(type), u.shape[2], u.shape[1],
+                               u.shape[0])
+    if np.isnan(r):
+        check_status(-1, cilreg)
+    return E_val

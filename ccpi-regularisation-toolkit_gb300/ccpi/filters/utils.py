@@ -38,6 +38,10 @@ _CPU_SIGS = {
     "TGV_main": [_P, _P, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I],
     "Diffusion_CPU_main": [_P, _P, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I],
     "Diffus4th_CPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I],
+    "LLT_ROF_CPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I],
+    "dTV_FGP_CPU_main": [_P, _P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I],
+    "TV_energy2D": [_P, _P, _P, _F, _I, _I, _I],
+    "TV_energy3D": [_P, _P, _P, _F, _I, _I, _I, _I],
 }
 # *_GPU_main argument lists (src/Core/regularisers_GPU/*.h)
 _GPU_SIGS = {
@@ -48,6 +52,8 @@ _GPU_SIGS = {
     "TGV_GPU_main": [_P, _P, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I, _I],
     "NonlDiff_GPU_main": [_P, _P, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I, _I],
     "Diffus4th_GPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I, _I],
+    "LLT_ROF_GPU_main": [_P, _P, _P, _F, _F, _I, _F, _F, _I, _I, _I, _I],
+    "dTV_FGP_GPU_main": [_P, _P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I, _I],
 }
 # device-pointer API (include/cilreg_gb300.h)
 _DEV_SIGS = {
@@ -58,6 +64,9 @@ _DEV_SIGS = {
     "cilreg_tgv_dev": [_V, _V, _P, _F, _F, _F, _I, _F, _F, _I, _I, _I, _V],
     "cilreg_ndf_dev": [_V, _V, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I, _V],
     "cilreg_diff4th_dev": [_V, _V, _P, _F, _F, _I, _F, _F, _I, _I, _I, _V],
+    "cilreg_llt_rof_dev": [_V, _V, _P, _F, _F, _I, _F, _F, _I, _I, _I, _V],
+    "cilreg_dtv_fgp_dev": [_V, _V, _V, _P, _F, _I, _F, _F, _I, _I, _I, _I, _I, _V],
+    "cilreg_tv_energy_dev": [_V, _V, _P, _F, _I, _I, _I, _I, _V],
 }
 
 _PP = ctypes.POINTER(ctypes.c_void_p)

@@ -135,6 +135,22 @@ int cilreg_diff4th_dev(const float* d_in, float* d_out, float* infovector, float
                        (cudaStream_t)stream, infovector);
 }
 
+int cilreg_llt_rof_dev(const float* d_in, float* d_out, float* infovector, float lambdaROF, float lambdaLLT,
+                       int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    return llt_run(d_in, d_out, lambdaROF, lambdaLLT, iters, tau, epsil, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
+int cilreg_dtv_fgp_dev(const float* d_in, const float* d_ref, float* d_out, float* infovector, float lambdaPar,
+                       int iters, float epsil, float eta, int methodTV, int nonneg, int dimX, int dimY, int dimZ,
+                       void* stream) {
+    CILREG_TRY(dev_prologue(d_in, d_out, dimX, dimY, dimZ));
+    if (!d_ref) return fail(ERR_ARG, __FILE__, __LINE__, "null reference image");
+    return dtv_run(d_in, d_ref, d_out, lambdaPar, iters, epsil, eta, methodTV, nonneg, dims_of(dimX, dimY, dimZ),
+                   (cudaStream_t)stream, infovector);
+}
+
 // ---------------------------------------------------------------------------
 // *_GPU_main: the reference GPU ABI (host pointers)
 int TV_ROF_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iter, float tau, float epsil,
@@ -204,6 +220,32 @@ int Diffus4th_GPU_main(float* Input, float* Output, float* infovector, float lam
     });
 }
 
+int LLT_ROF_GPU_main(float* Input, float* Output, float* infovector, float lambdaROF, float lambdaLLT,
+                     int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z) {
+    CILREG_TRY(check_dims(N, M, Z));
+    const Dims d = dims_of(N, M, Z);
+    return host_call(Input, Output, gpu_device, d, false, [&](const float* di, float* dout, cudaStream_t s) {
+        return llt_run(di, dout, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil, d, s, infovector);
+    });
+}
+
+int dTV_FGP_GPU_main(float* Input, float* InputRef, float* Output, float* infovector, float lambdaPar, int iter,
+                     float epsil, float eta, int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ) {
+    CILREG_TRY(check_dims(dimX, dimY, dimZ));
+    if (!InputRef) return fail(ERR_ARG, __FILE__, __LINE__, "null InputRef pointer");
+    const Dims d = dims_of(dimX, dimY, dimZ);
+    // as FGP: with a stopping rule the caller's Output is U_prev of iteration 0
+    return host_call(Input, Output, gpu_device, d, epsil != 0.0f || iter <= 0,
+                     [&](const float* di, float* dout, cudaStream_t s) {
+                         Scratch sc(s);
+                         float* dr = sc.floats(d.n);
+                         if (!dr) return sc.status();
+                         CILREG_CUDA(cudaMemcpyAsync(dr, InputRef, sizeof(float) * d.n, cudaMemcpyHostToDevice, s));
+                         return dtv_run(di, dr, dout, lambdaPar, iter, epsil, eta, methodTV, nonneg, d, s,
+                                        infovector);
+                     });
+}
+
 // ---------------------------------------------------------------------------
 // *_CPU_main: the reference C-OMP ABI, executed on the GPU
 float TV_ROF_CPU_main(float* Input, float* Output, float* infovector, float* lambdaPar, int lambda_is_arr,
@@ -256,6 +298,20 @@ float Diffus4th_CPU_main(float* Input, float* Output, float* infovector, float l
                          int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ) {
     return (float)Diffus4th_GPU_main(Input, Output, infovector, lambdaPar, sigmaPar, iterationsNumb, tau, epsil,
                                      default_device(), dimX, dimY, dimZ);
+}
+
+
+float LLT_ROF_CPU_main(float* Input, float* Output, float* infovector, float lambdaROF, float lambdaLLT,
+                       int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ) {
+    return (float)LLT_ROF_GPU_main(Input, Output, infovector, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil,
+                                   default_device(), dimX, dimY, dimZ);
+}
+
+float dTV_FGP_CPU_main(float* Input, float* InputRef, float* Output, float* infovector, float lambdaPar,
+                       int iterationsNumb, float epsil, float eta, int methodTV, int nonneg, int dimX, int dimY,
+                       int dimZ) {
+    return (float)dTV_FGP_GPU_main(Input, InputRef, Output, infovector, lambdaPar, iterationsNumb, epsil, eta,
+                                   methodTV, nonneg, default_device(), dimX, dimY, dimZ);
 }
 
 }  // extern "C"

@@ -64,6 +64,15 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
 int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, float epsil,
                 const Dims& d, cudaStream_t s, float* info);
 
+// FGP_dTV_core.c:46-180.  ref: the reference image (device); u_out's initial
+// content is U_prev of iteration 0, as for FGP
+int dtv_run(const float* f, const float* ref, float* u_out, float lam, int iters, float epsil, float eta,
+            int methodTV, int nonneg, const Dims& d, cudaStream_t s, float* info);
+
+// LLT_ROF_core.c:54-117
+int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iters, float tau, float epsil,
+            const Dims& d, cudaStream_t s, float* info);
+
 // shape validation shared by every entry point
 int check_dims(int nx, int ny, int nz);
 

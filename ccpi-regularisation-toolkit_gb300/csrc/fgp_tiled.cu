@@ -39,12 +39,16 @@ struct TiledArgs {
     float* u;
     float lam, c, multip;
     int nonneg, aniso, write_u, write_p, check;
+    const float* b[3];  // FGP-dTV only: unit gradient field of the reference image
 };
 
 // One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk.
 // CHECK: a stopping check (reads U_prev; the caller reduces the returned
 // per-thread sums).  IT: element-offset type (int below 2^31 voxels).
-template <bool THREE, bool CHECK, typename IT>
+// DTV: the FGP-dTV iteration (FGP_dTV_core.c:92-120): R and the gradient of U
+// are projected onto the orthogonal complement of a.b at each voxel
+// (ProjectVect_func, Grad_dfunc: FGP_dTV_core.c:302-363).
+template <bool THREE, bool CHECK, typename IT, bool DTV = false>
 __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& d, int zc, int bx, int by, int bz,
                                                 float& pa_out, float& pb_out) {
     __shared__ float sR1[BY][BX];
@@ -64,6 +68,7 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
 
     // prefetch registers for one plane
     float c1 = 0.f, o1 = 0.f, c2 = 0.f, o2 = 0.f, c3 = 0.f, o3 = 0.f, fv = 0.f;
+    float e1 = 0.f, e2 = 0.f, e3 = 0.f;  // dTV: unit gradient of the reference
     auto load_plane = [&](int k) {
         if (in_xy && k >= 0 && k < nz) {
             const IT v = (IT)k * sxy + col;
@@ -76,21 +81,36 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
                 o3 = __ldg(a.po[2] + v);
             }
             fv = __ldg(a.f + v);
+            if (DTV) {
+                e1 = __ldg(a.b[0] + v);
+                e2 = __ldg(a.b[1] + v);
+                if (THREE) e3 = __ldg(a.b[2] + v);
+            }
         } else {
             c1 = o1 = c2 = o2 = c3 = o3 = fv = 0.f;
+            e1 = e2 = e3 = 0.f;
         }
     };
 
     float r1p = 0.f, r2p = 0.f, r3p = 0.f, up = 0.f;  // R and U of plane k-1 at this voxel
+    float b1p = 0.f, b2p = 0.f, b3p = 0.f;            // dTV: unit gradient of plane k-1
     float uo = 0.f;  // U_prev of the plane the next P step writes (stopping checks only)
     float pa = 0.f, pb = 0.f;
     load_plane(z0 - 1);
     for (int k = z0 - 1; k <= z1; ++k) {
         // 1. R of plane k from the prefetched values; start loading plane k+1
-        const float r1 = c1 + a.c * (c1 - o1);
-        const float r2 = c2 + a.c * (c2 - o2);
-        const float r3 = THREE ? (c3 + a.c * (c3 - o3)) : 0.f;
+        float r1 = c1 + a.c * (c1 - o1);
+        float r2 = c2 + a.c * (c2 - o2);
+        float r3 = THREE ? (c3 + a.c * (c3 - o3)) : 0.f;
         const float fk = fv;
+        const float b1 = e1, b2 = e2, b3 = e3;
+        if (DTV) {
+            // R onto the complement of the reference's unit gradient (FGP_dTV_core.c:311-314)
+            const float ip = THREE ? (r1 * b1 + r2 * b2 + r3 * b3) : (r1 * b1 + r2 * b2);
+            r1 = r1 - ip * b1;
+            r2 = r2 - ip * b2;
+            if (THREE) r3 = r3 - ip * b3;
+        }
         if (k < z1) load_plane(k + 1);
         // U_prev of plane k, consumed one plane later: loaded here so that its
         // latency overlaps the barriers instead of stalling the P step
@@ -124,15 +144,20 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
             if (a.write_u) a.u[v] = up;
             if (a.write_p) {
                 const int ps = kp & 1;
-                const float g1 = (x == nx - 1) ? 0.f : up - sU[ps][ty][tx + 1];
-                const float g2 = (y == ny - 1) ? 0.f : up - sU[ps][ty + 1][tx];
+                float g1 = (x == nx - 1) ? 0.f : up - sU[ps][ty][tx + 1];
+                float g2 = (y == ny - 1) ? 0.f : up - sU[ps][ty + 1][tx];
+                float g3 = (THREE && kp != nz - 1) ? up - u : 0.f;
+                if (DTV) {
+                    // gradient onto the complement of the unit gradient (FGP_dTV_core.c:350-356)
+                    const float ip = THREE ? (g1 * b1p + g2 * b2p + g3 * b3p) : (g1 * b1p + g2 * b2p);
+                    g1 = g1 - ip * b1p;
+                    g2 = g2 - ip * b2p;
+                    if (THREE) g3 = g3 - ip * b3p;
+                }
                 float p1 = r1p + a.multip * g1;
                 float p2 = r2p + a.multip * g2;
                 float p3 = 0.f;
-                if (THREE) {
-                    const float g3 = (kp == nz - 1) ? 0.f : up - u;
-                    p3 = r3p + a.multip * g3;
-                }
+                if (THREE) p3 = r3p + a.multip * g3;
                 if (!a.aniso) {
                     const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
                     const float sq = (den > 1.f) ? rsqrtf(den) : 1.f;  // within 2 ulp of 1/sqrtf
@@ -152,6 +177,11 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
         r1p = r1;
         r2p = r2;
         r3p = r3;
+        if (DTV) {
+            b1p = b1;
+            b2p = b2;
+            b3p = b3;
+        }
         up = u;
         uo = uo_next;
     }
@@ -159,12 +189,12 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
     pb_out = pb;
 }
 
-template <bool THREE, bool CHECK, typename IT>
-__global__ void __launch_bounds__(NT, 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
-                                                      double2* partials) {
+template <bool THREE, bool CHECK, typename IT, bool DTV = false>
+__global__ void __launch_bounds__(NT, DTV ? 2 : 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
+                                                                double2* partials) {
     if (ctl->stop) return;
     float pa = 0.f, pb = 0.f;
-    fgp_stream_tile<THREE, CHECK, IT>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
+    fgp_stream_tile<THREE, CHECK, IT, DTV>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
@@ -195,6 +225,7 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* _
     a.write_u = write_u;
     a.write_p = write_p;
     a.check = CHECK;
+    a.b[0] = a.b[1] = a.b[2] = nullptr;
     float pa = 0.f, pb = 0.f;
     fgp_stream_tile<THREE, CHECK, IT>(a, V.d, V.zc, bx, by, bz, pa, pb);
     if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
@@ -249,7 +280,8 @@ TiledPlan fgp_tiled_plan(const Dims& d) {
 
 int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
-                   int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s) {
+                   int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
+                   const float* const* b) {
     TiledArgs a;
     for (int i = 0; i < 3; i++) {
         a.pc[i] = pc[i];
@@ -266,9 +298,19 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
     a.write_u = write_u;
     a.write_p = write_p;
     a.check = check;
+    for (int i = 0; i < 3; i++) a.b[i] = b ? b[i] : nullptr;
     const bool three = d.nz > 1;
     decltype(&k_fgp_stream<true, true, int>) kern;
-    if (d.n < (1LL << 31))
+    if (b) {
+        if (d.n < (1LL << 31))
+            kern = three ? (check ? k_fgp_stream<true, true, int, true> : k_fgp_stream<true, false, int, true>)
+                         : (check ? k_fgp_stream<false, true, int, true> : k_fgp_stream<false, false, int, true>);
+        else
+            kern = three ? (check ? k_fgp_stream<true, true, long long, true>
+                                  : k_fgp_stream<true, false, long long, true>)
+                         : (check ? k_fgp_stream<false, true, long long, true>
+                                  : k_fgp_stream<false, false, long long, true>);
+    } else if (d.n < (1LL << 31))
         kern = three ? (check ? k_fgp_stream<true, true, int> : k_fgp_stream<true, false, int>)
                      : (check ? k_fgp_stream<false, true, int> : k_fgp_stream<false, false, int>);
     else

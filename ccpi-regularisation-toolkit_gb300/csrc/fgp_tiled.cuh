@@ -15,9 +15,12 @@ struct TiledPlan {
 TiledPlan fgp_tiled_plan(const Dims& d);
 int fgp_default_zchunk(const Dims& d);
 
+// one FGP iteration; with `b` (three device arrays, the unit gradient field
+// of a reference image) one FGP-dTV iteration instead
 int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
-                   int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s);
+                   int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
+                   const float* const* b = nullptr);
 
 // One volume of a batched FGP run (device-resident descriptor table).
 struct FgpBatchVol {

@@ -69,6 +69,15 @@ int NonlDiff_GPU_main(float *Input, float *Output, float *infovector, float lamb
 int Diffus4th_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
                        int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z);
 
+/* replaces LLT_ROF_GPU_main, src/Core/regularisers_GPU/LLT_ROF_GPU_core.h:6 */
+int LLT_ROF_GPU_main(float *Input, float *Output, float *infovector, float lambdaROF, float lambdaLLT,
+                     int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z);
+
+/* replaces dTV_FGP_GPU_main, src/Core/regularisers_GPU/dTV_FGP_GPU_core.h:7.
+ * As in the CPU reference, Output's initial content is U_prev of iteration 0. */
+int dTV_FGP_GPU_main(float *Input, float *InputRef, float *Output, float *infovector, float lambdaPar, int iter,
+                     float epsil, float eta, int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ);
+
 /* ---------------------------------------------------------------------------
  * Reference C-OMP ABI.  Same argument lists and return type as the
  * reference; the work runs on GPU CILREG_GPU_DEVICE (environment, default 0).
@@ -103,6 +112,23 @@ float Diffusion_CPU_main(float *Input, float *Output, float *infovector, float l
 float Diffus4th_CPU_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
                          int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ);
 
+/* replaces LLT_ROF_CPU_main, src/Core/regularisers_CPU/LLT_ROF_core.h:52 */
+float LLT_ROF_CPU_main(float *Input, float *Output, float *infovector, float lambdaROF, float lambdaLLT,
+                       int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ);
+
+/* replaces dTV_FGP_CPU_main, src/Core/regularisers_CPU/FGP_dTV_core.h:56 */
+float dTV_FGP_CPU_main(float *Input, float *InputRef, float *Output, float *infovector, float lambdaPar,
+                       int iterationsNumb, float epsil, float eta, int methodTV, int nonneg, int dimX, int dimY,
+                       int dimZ);
+
+/* replace TV_energy2D / TV_energy3D, src/Core/regularisers_CPU/utils.h:30-31.
+ * Writes E_val[0] and returns it; type 1: 2 lambda TV(U) + |U - U0|^2, type 2:
+ * 2 lambda TV(U).  Terms summed in double (the reference sums sequentially in
+ * float).  On failure E_val[0] and the return value are NaN and
+ * cilreg_last_error() says why. */
+float TV_energy2D(float *U, float *U0, float *E_val, float lambda, int type, int dimX, int dimY);
+float TV_energy3D(float *U, float *U0, float *E_val, float lambda, int type, int dimX, int dimY, int dimZ);
+
 /* ---------------------------------------------------------------------------
  * Device-pointer API.  d_in / d_out are distinct device buffers of
  * dimX*dimY*dimZ floats on the current device; `stream` is a cudaStream_t
@@ -128,6 +154,15 @@ int cilreg_ndf_dev(const float *d_in, float *d_out, float *infovector, float lam
                    float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ, void *stream);
 int cilreg_diff4th_dev(const float *d_in, float *d_out, float *infovector, float lambdaPar, float sigmaPar,
                        int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
+int cilreg_llt_rof_dev(const float *d_in, float *d_out, float *infovector, float lambdaROF, float lambdaLLT,
+                       int iters, float tau, float epsil, int dimX, int dimY, int dimZ, void *stream);
+/* d_ref: the reference image (device) of FGP-dTV */
+int cilreg_dtv_fgp_dev(const float *d_in, const float *d_ref, float *d_out, float *infovector, float lambdaPar,
+                       int iters, float epsil, float eta, int methodTV, int nonneg, int dimX, int dimY, int dimZ,
+                       void *stream);
+/* TV energy of device arrays; E_val is a host pointer to one float */
+int cilreg_tv_energy_dev(const float *d_u, const float *d_u0, float *E_val, float lambda, int type, int dimX,
+                         int dimY, int dimZ, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Batched API (no counterpart in the reference, whose callers loop over

@@ -853,7 +853,8 @@ float port_LLT_ROF(float *Input, float *Output, float *infovector, float lambdaR
         idx_t i, j, k;
         if (check) copy_arr(Output, Uprev, n);
         rof_fluxes(Output, R1, R2, R3, nx, ny, nz, 1.0e-12);
-        /* der2D_LLT / der3D_LLT (LLT_ROF_core.c:131-188): dxx / (|dxx| + 1e-12) */
+        /* der2D_LLT / der3D_LLT (LLT_ROF_core.c:131-188): dxx / (|dxx| + 1e-12),
+         * the denominator formed in double and stored in a float */
 #pragma omp parallel for private(i, j)
         for (k = 0; k < nz; k++)
             for (j = 0; j < ny; j++)
@@ -862,11 +863,11 @@ float port_LLT_ROF(float *Input, float *Output, float *infovector, float lambdaR
                     float u = Output[v];
                     float dxx = Output[s * k + nx * j + nb_hi(i, nx)] - 2.0f * u + Output[s * k + nx * j + nb_lo(i, nx)];
                     float dyy = Output[s * k + nx * nb_hi(j, ny) + i] - 2.0f * u + Output[s * k + nx * nb_lo(j, ny) + i];
-                    L1[v] = (float)(dxx / (fabs(dxx) + 1.0e-12));
-                    L2[v] = (float)(dyy / (fabs(dyy) + 1.0e-12));
+                    L1[v] = dxx / (float)(fabs(dxx) + 1.0e-12);
+                    L2[v] = dyy / (float)(fabs(dyy) + 1.0e-12);
                     if (three) {
                         float dzz = Output[s * nb_hi(k, nz) + nx * j + i] - 2.0f * u + Output[s * nb_lo(k, nz) + nx * j + i];
-                        L3[v] = (float)(dzz / (fabs(dzz) + 1.0e-12));
+                        L3[v] = dzz / (float)(fabs(dzz) + 1.0e-12);
                     }
                 }
         /* Update2D_LLT_ROF / Update3D_LLT_ROF (LLT_ROF_core.c:377-436) */

@@ -41,7 +41,16 @@ _BASE = [
     _c("ndf_stop", "ndf", lam=0.02, sigma=0.05, iters=300, tau=0.01, penalty=1, epsil=1e-3),
     _c("d4", "d4", lam=0.8, sigma=0.02, iters=120, tau=1e-4, epsil=0.0),
     _c("d4_stop", "d4", lam=0.8, sigma=0.02, iters=300, tau=1e-4, epsil=1e-3),
+    # next-tier regularisers (reference test/test_2d_cpu_vs_gpu.py:361-377, 549-565)
+    _c("llt_rof", "llt", lam_rof=0.02, lam_llt=0.01, iters=200, tau=0.001, epsil=0.0),
+    _c("llt_rof_stop", "llt", lam_rof=0.02, lam_llt=0.01, iters=300, tau=0.001, epsil=1e-3),
+    _c("dtv_iso", "dtv", lam=0.05, iters=120, epsil=0.0, eta=0.2, method=0, nonneg=0),
+    _c("dtv_aniso_nonneg", "dtv", lam=0.05, iters=120, epsil=0.0, eta=0.2, method=1, nonneg=1),
+    _c("dtv_stop", "dtv", lam=0.05, iters=300, epsil=3e-4, eta=0.2, method=0, nonneg=1),
 ]
+
+# TV energy cases (lambda, type) on (input, reference image)
+ENERGY = [(0.1, 1), (0.1, 2), (0.03, 1)]
 
 
 def cases():
@@ -62,12 +71,26 @@ def make_input(dim: int):
     return noisy_phantom(SHAPE_2D if dim == 2 else SHAPE_3D, n, seed)
 
 
-def run_oracle(case, x, use_ref=False, jacobi=True):
+def make_ref(dim: int):
+    """The FGP-dTV reference image: the noise-free phantom behind make_input."""
+    from ccpi.supp.phantoms import clean_phantom
+
+    n, seed = SEEDS[dim]
+    return clean_phantom(SHAPE_2D if dim == 2 else SHAPE_3D, n, seed)
+
+
+def run_oracle(case, x, use_ref=False, jacobi=True, ref=None):
     """Run `case` on the oracle (port, or the compiled reference)."""
     import oracle as O
 
     p = case["params"]
     a = case["alg"]
+    if a == "llt":
+        return O.llt_rof(x, p["lam_rof"], p["lam_llt"], p["iters"], p["tau"], p["epsil"], use_ref=use_ref)
+    if a == "dtv":
+        r = make_ref(case["dim"]) if ref is None else ref
+        return O.dtv_fgp(x, r, p["lam"], p["iters"], p["epsil"], p["eta"], p["method"], p["nonneg"],
+                         use_ref=use_ref)
     if a == "rof":
         return O.rof_tv(x, p["lam"], p["iters"], p["tau"], p["epsil"], use_ref=use_ref)
     if a == "fgp":
@@ -86,7 +109,7 @@ def run_oracle(case, x, use_ref=False, jacobi=True):
     raise KeyError(a)
 
 
-def run_gpu(case, x, api="gpu", device=0):
+def run_gpu(case, x, api="gpu", device=0, ref=None):
     """Run `case` through the product's Python API.  api: 'gpu' (the *_GPU_main
     argument list), 'cpu' (the *_CPU_main list, which also runs on the GPU)."""
     import numpy as np
@@ -117,6 +140,13 @@ def run_gpu(case, x, api="gpu", device=0):
                     infovector=info)
     elif a == "d4":
         out = R.Diff4th(x, p["lam"], p["sigma"], p["iters"], p["tau"], p["epsil"], device=dev, infovector=info)
+    elif a == "llt":
+        out = R.LLT_ROF(x, p["lam_rof"], p["lam_llt"], p["iters"], p["tau"], p["epsil"], device=dev,
+                        infovector=info)
+    elif a == "dtv":
+        r = make_ref(case["dim"]) if ref is None else ref
+        out = R.FGP_dTV(x, r, p["lam"], p["iters"], p["epsil"], p["eta"], p["method"], p["nonneg"], device=dev,
+                        infovector=info)
     else:
         raise KeyError(a)
     return out, info

@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference toolkit's own C-OMP code.
 
 Runs every case of ``cases.py`` through ``oracle/_ref/libcilreg_ref.so`` (the
-reference sources compiled by ``make -C oracle ref``) and stores inputs,
-outputs and infovectors in ``reference_outputs.npz``.  The reference's
+reference sources compiled by ``make -C oracle ref``) and stores inputs (and
+the FGP-dTV reference images), outputs, infovectors and TV energies in
+``reference_outputs.npz``.  The reference's
 non-linear diffusion updates in place, so it is run with one OpenMP thread
 (lexicographic order), the only deterministic setting.
 
@@ -33,9 +34,14 @@ def main():
     arrays = {}
     for dim in (2, 3):
         arrays[f"input_{dim}d"] = C.make_input(dim)
+        arrays[f"ref_{dim}d"] = C.make_ref(dim)
+        for lam, typ in C.ENERGY:
+            e = O.tv_energy(arrays[f"input_{dim}d"], arrays[f"ref_{dim}d"], lam, typ, use_ref=True)
+            arrays[f"energy_{dim}d_{lam}_{typ}"] = np.float32(e)
+            print(f"energy {dim}d lambda={lam} type={typ}: {e!r}")
     for case in C.cases():
         x = arrays[f"input_{case['dim']}d"]
-        out, info = C.run_oracle(case, x, use_ref=True)
+        out, info = C.run_oracle(case, x, use_ref=True, ref=arrays[f"ref_{case['dim']}d"])
         arrays[f"out_{case['key']}"] = out
         arrays[f"info_{case['key']}"] = info
         print(f"{case['key']:24s} iters={int(info[0]):4d} re={info[1]:.3e}")

@@ -106,7 +106,7 @@ def test_output_validation():
 def test_out_of_scope_regularisers_raise():
     from ccpi.filters import regularisers as R
 
-    for fn in (R.LLT_ROF, R.FGP_dTV, R.PatchSelect):
+    for fn in (R.PatchSelect, R.NLTV, R.TNV):
         with pytest.raises(NotImplementedError):
             fn(np.zeros((4, 4), np.float32))
 

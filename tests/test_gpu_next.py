@@ -1,0 +1,126 @@
+"""GPU tests of the next-tier entry points (LLT-ROF, FGP-dTV, TV energy)
+beyond the golden cases of test_gpu_parity.py: odd shapes against the oracle
+port, the host and device APIs against each other, and the energy against
+the reference's own values."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cases as C
+import oracle as O
+from conftest import rel_tol
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9), (130, 33, 35)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=str)
+def test_llt_rof_matches_oracle_on_odd_shapes(shape):
+    from ccpi.filters.regularisers import LLT_ROF
+
+    rng = np.random.default_rng(41 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil in (0.0, 1e-3):
+        ref, iref = O.llt_rof(x, 0.02, 0.01, 80, 0.001, epsil)
+        info = np.zeros(2, np.float32)
+        got = LLT_ROF(x, 0.02, 0.01, 80, 0.001, epsil, device="gpu", infovector=info)
+        assert int(info[0]) == int(iref[0])
+        assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-4)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=str)
+def test_fgp_dtv_matches_oracle_on_odd_shapes(shape):
+    from ccpi.filters.regularisers import FGP_dTV
+
+    rng = np.random.default_rng(43 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    r = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0)):
+        ref, iref = O.dtv_fgp(x, r, 0.05, 80, epsil, 0.2, method, nonneg)
+        info = np.zeros(2, np.float32)
+        got = FGP_dTV(x, r, 0.05, 80, epsil, 0.2, method, nonneg, device="gpu", infovector=info)
+        assert int(info[0]) == int(iref[0])
+        assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-4)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("lam,typ", C.ENERGY)
+def test_tv_energy_matches_reference(dim, lam, typ, golden):
+    """The reference sums sequentially in FP32, the GPU in FP64: equal to 1e-5."""
+    from ccpi.filters.regularisers import TV_ENERGY
+
+    u, u0 = golden[f"input_{dim}d"], golden[f"ref_{dim}d"]
+    e = float(TV_ENERGY(u, u0, lam, typ)[0])
+    ref = float(golden[f"energy_{dim}d_{lam}_{typ}"])
+    assert abs(e - ref) <= 1e-5 * abs(ref)
+    exact = O.tv_energy(u.astype(np.float64).astype(np.float32), u0, lam, typ)  # port, same terms
+    assert abs(e - exact) <= 1e-5 * abs(exact)
+
+
+def test_tv_energy_large_volume_against_float64_sum():
+    """At 2^24 voxels the FP64 accumulation stays at FP32 term rounding."""
+    from ccpi.filters.regularisers import TV_ENERGY
+
+    rng = np.random.default_rng(5)
+    u = rng.random((256, 256, 256), dtype=np.float32)
+    u0 = rng.random((256, 256, 256), dtype=np.float32)
+    e = float(TV_ENERGY(u, u0, 0.1, 1)[0])
+    ud = u.astype(np.float64)
+    gx = np.diff(ud, axis=2, append=ud[:, :, -1:])
+    gy = np.diff(ud, axis=1, append=ud[:, -1:, :])
+    gz = np.diff(ud, axis=0, append=ud[-1:, :, :])
+    exact = 2 * 0.1 * np.sqrt(gx * gx + gy * gy + gz * gz).sum() + ((ud - u0) ** 2).sum()
+    assert abs(e - exact) <= 1e-6 * abs(exact)
+
+
+def test_device_api_matches_host_api():
+    import torch
+
+    from ccpi.filters import utils as U
+    from ccpi.filters.regularisers import FGP_dTV, LLT_ROF, TV_ENERGY
+
+    rng = np.random.default_rng(9)
+    x = rng.random((12, 40, 36)).astype(np.float32)
+    r = rng.random((12, 40, 36)).astype(np.float32)
+    dims = (36, 40, 12)
+    s = torch.cuda.current_stream().cuda_stream
+    dx, dr = torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda()
+    info = (ctypes.c_float * 2)()
+
+    out = torch.zeros_like(dx)
+    U.check_status(U.cilregcuda.cilreg_llt_rof_dev(dx.data_ptr(), out.data_ptr(), info, 0.02, 0.01, 50, 0.001, 0.0,
+                                                   *dims, s))
+    np.testing.assert_array_equal(out.cpu().numpy(), LLT_ROF(x, 0.02, 0.01, 50, 0.001, 0.0, device="gpu"))
+
+    out = torch.zeros_like(dx)
+    U.check_status(U.cilregcuda.cilreg_dtv_fgp_dev(dx.data_ptr(), dr.data_ptr(), out.data_ptr(), info, 0.05, 50,
+                                                   0.0, 0.2, 0, 1, *dims, s))
+    np.testing.assert_array_equal(out.cpu().numpy(), FGP_dTV(x, r, 0.05, 50, 0.0, 0.2, 0, 1, device="gpu"))
+
+    e = (ctypes.c_float * 1)()
+    U.check_status(U.cilregcuda.cilreg_tv_energy_dev(dx.data_ptr(), dr.data_ptr(), e, 0.1, 1, *dims, s))
+    assert e[0] == TV_ENERGY(x, r, 0.1, 1)[0]
+
+
+def test_cpu_abi_is_the_same_gpu_code():
+    from ccpi.filters.regularisers import FGP_dTV, LLT_ROF
+
+    rng = np.random.default_rng(10)
+    x = rng.random((9, 30, 33)).astype(np.float32)
+    r = rng.random((9, 30, 33)).astype(np.float32)
+    np.testing.assert_array_equal(LLT_ROF(x, 0.02, 0.01, 40, 0.001, 1e-3, device="cpu"),
+                                  LLT_ROF(x, 0.02, 0.01, 40, 0.001, 1e-3, device="gpu"))
+    np.testing.assert_array_equal(FGP_dTV(x, r, 0.05, 40, 1e-4, 0.2, 0, 1, device="cpu"),
+                                  FGP_dTV(x, r, 0.05, 40, 1e-4, 0.2, 0, 1, device="gpu"))
+
+
+def test_invalid_arguments_raise():
+    from ccpi.filters.regularisers import FGP_dTV, TV_ENERGY
+
+    x = np.zeros((8, 9), np.float32)
+    with pytest.raises(ValueError):
+        FGP_dTV(x, np.zeros((9, 8), np.float32), 0.05, 10, 0.0, 0.2, 0, 0, device="gpu")
+    with pytest.raises(ValueError):
+        TV_ENERGY(x, x, 0.1, 3)

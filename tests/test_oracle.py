@@ -118,3 +118,19 @@ def test_port_matches_live_reference_llt_dtv_energy(shape):
             np.testing.assert_array_equal(ia, ib)
     for typ in (1, 2):
         assert O.tv_energy(x, ref, 0.1, typ) == O.tv_energy(x, ref, 0.1, typ, use_ref=True)
+
+
+def test_fixture_reference_images_are_the_clean_phantoms(golden):
+    for dim in (2, 3):
+        np.testing.assert_array_equal(C.make_ref(dim), golden[f"ref_{dim}d"])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("lam,typ", C.ENERGY)
+def test_port_energy_matches_reference_fixture(dim, lam, typ, golden):
+    e = O.tv_energy(golden[f"input_{dim}d"], golden[f"ref_{dim}d"], lam, typ)
+    ref = float(golden[f"energy_{dim}d_{lam}_{typ}"])
+    if _bit_exact_platform():
+        assert np.float32(e) == np.float32(ref)
+    else:
+        assert abs(e - ref) <= 1e-5 * abs(ref)
