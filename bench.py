@@ -208,6 +208,8 @@ def profile_case(args):
         "TGV": lambda: D.TGV(d_in, 0.03, 1.0, 2.0, args.iters, 12.0),
         "NDF": lambda: D.NDF(d_in, 0.02, 0.02, args.iters, 0.01, 1),
         "Diff4th": lambda: D.Diff4th(d_in, 0.8, 0.02, args.iters, 1e-4),
+        "LLT_ROF": lambda: D.LLT_ROF(d_in, 0.02, 0.01, args.iters, 0.001),
+        "FGP_dTV": lambda: D.FGP_dTV(d_in, d_in, 0.03, args.iters, 0.0, 0.2, 0, 1),
     }
     times = []
     for k in range(args.warmup + args.steps):
@@ -232,7 +234,7 @@ def profile_case(args):
 
 # algorithmic bytes per voxel-iteration of each regulariser's fused iteration
 SUITE_BYTES = {"ROF": (12, 12), "FGP": (40, 28), "PD": (36, 28), "SB": (60, 44), "TGV": (108, 68), "NDF": (12, 12),
-               "Diff4th": (12, 12)}
+               "Diff4th": (12, 12), "LLT_ROF": (12, 12), "FGP_dTV": (52, 36)}
 
 
 def suite(args):
@@ -252,6 +254,8 @@ def suite(args):
         "TGV": lambda t, n: D.TGV(t, 0.03, 1.0, 2.0, n, 12.0),
         "NDF": lambda t, n: D.NDF(t, 0.02, 0.02, n, 0.01, 1),
         "Diff4th": lambda t, n: D.Diff4th(t, 0.8, 0.02, n, 1e-4),
+        "LLT_ROF": lambda t, n: D.LLT_ROF(t, 0.02, 0.01, n, 0.001),
+        "FGP_dTV": lambda t, n: D.FGP_dTV(t, t, 0.03, n, 0.0, 0.2, 0, 1),
     }
     shapes = [(256, 256, 256), (512, 512)] if args.size <= 256 else [(args.size,) * 3, (512, 512)]
     rows = []
@@ -506,7 +510,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
     ap.add_argument("--iters", type=int, default=20, help="iterations per call in --profile-case")
-    ap.add_argument("--reg", default="FGP", help="regulariser of --profile-case (FGP, ROF, PD, SB, TGV, NDF, Diff4th)")
+    ap.add_argument("--reg", default="FGP",
+                    help="regulariser of --profile-case (FGP, ROF, PD, SB, TGV, NDF, Diff4th, LLT_ROF, FGP_dTV)")
     ap.add_argument("--batch", action="store_true",
                     help="64 uneven volumes, FGP and TGV at 300 iterations: batched graph launch vs per-call")
     ap.add_argument("--autograd", action="store_true",

@@ -1,6 +1,6 @@
 """Device-array regularisers: the reference's src/Python/ccpi/filters/regularisersCuPy.py
 (ROF_TV :35-40, PD_TV :130-138) with the same signatures, extended to all
-seven regularisers.
+seven regularisers, LLT-ROF, FGP-dTV and the TV energy.
 
 Inputs are device arrays already resident on the GPU: CuPy arrays, torch
 CUDA tensors, or any object exposing ``__cuda_array_interface__`` (float32,
@@ -16,7 +16,7 @@ import numpy as np
 
 from .utils import check_status, cilregcuda
 
-__all__ = ["ROF_TV", "PD_TV", "FGP_TV", "SB_TV", "TGV", "NDF", "Diff4th"]
+__all__ = ["ROF_TV", "PD_TV", "FGP_TV", "SB_TV", "TGV", "NDF", "Diff4th", "LLT_ROF", "FGP_dTV", "TV_ENERGY"]
 
 
 def _is_torch(x):
@@ -142,3 +142,53 @@ def Diff4th(data, regularisation_parameter=1e-05, edge_parameter=0.01, iteration
     """Fourth-order diffusion on a device array."""
     return _call(cilregcuda.cilreg_diff4th_dev, data, gpu_id, infovector, float(regularisation_parameter),
                  float(edge_parameter), int(iterations), float(time_marching_parameter), float(tolerance_param))
+
+
+def LLT_ROF(data, regularisation_parameterROF=1e-05, regularisation_parameterLLT=1e-05, iterations=500,
+            time_marching_parameter=0.0001, tolerance_param=0.0, gpu_id=0, infovector=None):
+    """LLT-ROF on a device array."""
+    return _call(cilregcuda.cilreg_llt_rof_dev, data, gpu_id, infovector, float(regularisation_parameterROF),
+                 float(regularisation_parameterLLT), int(iterations), float(time_marching_parameter),
+                 float(tolerance_param))
+
+
+def _pointer_like(ref, data, shape):
+    """Device pointer of `ref`, which must match data's kind, shape and dtype."""
+    if _is_torch(data):
+        if not _is_torch(ref) or tuple(ref.shape) != shape or ref.dtype != data.dtype or ref.device != data.device:
+            raise ValueError("refdata must be a float32 CUDA tensor of the input's shape and device")
+        ref = ref.contiguous()
+        return ref, ref.data_ptr()
+    cai = getattr(ref, "__cuda_array_interface__", None)
+    if cai is None or tuple(cai["shape"]) != shape or np.dtype(cai["typestr"]) != np.float32:
+        raise ValueError("refdata must be a float32 device array of the input's shape")
+    return ref, int(cai["data"][0])
+
+
+def FGP_dTV(data, refdata, regularisation_parameter=1e-05, iterations=500, tolerance_param=0.0, eta_const=0.01,
+            methodTV=0, nonneg=0, gpu_id=0, infovector=None):
+    """FGP-dTV on device arrays (U_prev of iteration 0 is zero)."""
+    data, out, pin, pout, shape, stream = _prepare(data, gpu_id)
+    refdata, pref = _pointer_like(refdata, data, shape)
+    if _is_torch(out):
+        out.zero_()
+    else:
+        out.fill(0)
+    info = _info(infovector)
+    fn = cilregcuda.cilreg_dtv_fgp_dev
+    st = fn(pin, pref, pout, info.ctypes.data_as(fn.argtypes[3]), float(regularisation_parameter), int(iterations),
+            float(tolerance_param), float(eta_const), int(methodTV), int(nonneg), *_dims(shape), stream)
+    check_status(st)
+    return out
+
+
+def TV_ENERGY(data, data0, regularisation_parameter, type=1, gpu_id=0):
+    """TV energy of device arrays (type 1: 2 lambda TV + |u - u0|^2; type 2: 2 lambda TV); a float."""
+    data, _, pin, _, shape, stream = _prepare(data, gpu_id)
+    data0, p0 = _pointer_like(data0, data, shape)
+    e = np.zeros(1, np.float32)
+    fn = cilregcuda.cilreg_tv_energy_dev
+    st = fn(pin, p0, e.ctypes.data_as(fn.argtypes[2]), float(regularisation_parameter), int(type), *_dims(shape),
+            stream)
+    check_status(st)
+    return float(e[0])

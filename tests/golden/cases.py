@@ -71,12 +71,17 @@ def make_input(dim: int):
     return noisy_phantom(SHAPE_2D if dim == 2 else SHAPE_3D, n, seed)
 
 
-def make_ref(dim: int):
-    """The FGP-dTV reference image: the noise-free phantom behind make_input."""
+def make_ref(dim: int, shape=None):
+    """The FGP-dTV reference image: the noise-free phantom behind make_input
+    (of `shape` instead of the case shape when given)."""
     from ccpi.supp.phantoms import clean_phantom
 
     n, seed = SEEDS[dim]
-    return clean_phantom(SHAPE_2D if dim == 2 else SHAPE_3D, n, seed)
+    return clean_phantom(shape or (SHAPE_2D if dim == 2 else SHAPE_3D), n, seed)
+
+
+def _ref_for(case, x, ref):
+    return make_ref(case["dim"], tuple(x.shape)) if ref is None else ref
 
 
 def run_oracle(case, x, use_ref=False, jacobi=True, ref=None):
@@ -88,7 +93,7 @@ def run_oracle(case, x, use_ref=False, jacobi=True, ref=None):
     if a == "llt":
         return O.llt_rof(x, p["lam_rof"], p["lam_llt"], p["iters"], p["tau"], p["epsil"], use_ref=use_ref)
     if a == "dtv":
-        r = make_ref(case["dim"]) if ref is None else ref
+        r = _ref_for(case, x, ref)
         return O.dtv_fgp(x, r, p["lam"], p["iters"], p["epsil"], p["eta"], p["method"], p["nonneg"],
                          use_ref=use_ref)
     if a == "rof":
@@ -144,7 +149,7 @@ def run_gpu(case, x, api="gpu", device=0, ref=None):
         out = R.LLT_ROF(x, p["lam_rof"], p["lam_llt"], p["iters"], p["tau"], p["epsil"], device=dev,
                         infovector=info)
     elif a == "dtv":
-        r = make_ref(case["dim"]) if ref is None else ref
+        r = _ref_for(case, x, ref)
         out = R.FGP_dTV(x, r, p["lam"], p["iters"], p["epsil"], p["eta"], p["method"], p["nonneg"], device=dev,
                         infovector=info)
     else:
