@@ -233,7 +233,10 @@ def profile_case(args):
 
 
 # algorithmic bytes per voxel-iteration of each regulariser's fused iteration
-SUITE_BYTES = {"ROF": (12, 12), "FGP": (40, 28), "PD": (36, 28), "SB": (60, 44), "TGV": (108, 68), "NDF": (12, 12),
+# algorithmic bytes per voxel-iteration (3D, 2D): each state array read and
+# written once, read-only inputs read once; SB's state is U and B (D is
+# recomputed from them), TGV's U, P, Q, V
+SUITE_BYTES = {"ROF": (12, 12), "FGP": (40, 28), "PD": (36, 28), "SB": (36, 28), "TGV": (108, 68), "NDF": (12, 12),
                "Diff4th": (12, 12), "LLT_ROF": (12, 12), "FGP_dTV": (52, 36)}
 
 

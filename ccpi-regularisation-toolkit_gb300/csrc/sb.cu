@@ -3,10 +3,16 @@
 // Per outer iteration: two Jacobi sweeps of the (mu + 2*dim*lambda) system
 // (the reference's gauss_seidel*, which read U_prev only), then shrinkage of
 // grad U + B into D and the Bregman update of B.  Kernels:
-//   k_sb_sweep2  both sweeps in one streaming pass (sb_tiled.cu)
+//   k_sb_sweep2  both sweeps of the first outer iteration in one streaming
+//                pass (sb_tiled.cu)
+//   k_sb_fused   every later outer iteration in one streaming pass: D and B
+//                formed from U and the previous B, both sweeps, new U and B
+//                written (sb_tiled.cu); D is never stored
 //   k_sb_sweep   U_out = sweep(U_in, D, B, f), x2 (CILREG_SB_KERNEL=simple,
 //                and volumes of 2^31 voxels or more)
-//   k_sb_shrink  D, B updated in place from the new U (one voxel each)
+//   k_sb_shrink  D, B updated in place from the new U (one voxel each): after
+//                every iteration of the per-sweep path, and once at the end
+//                of a warm-state (session) run of the streaming path
 // The stopping check compares the two sweeps' results (SB_TV_core.c:123-134).
 #include "drivers.cuh"
 #include "sb_tiled.cuh"
@@ -145,11 +151,16 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
             a.bb[c] = warm->bb[c];
             continue;
         }
-        a.dd[c] = scratch.floats(d.n);
         a.bb[c] = scratch.floats(d.n);
-        if (!a.dd[c] || !a.bb[c]) return scratch.status();
-        CILREG_CUDA(cudaMemsetAsync(a.dd[c], 0, sizeof(float) * d.n, s));
+        if (!a.bb[c]) return scratch.status();
         CILREG_CUDA(cudaMemsetAsync(a.bb[c], 0, sizeof(float) * d.n, s));
+        if (T.use) {
+            a.dd[c] = a.bb[c];  // D^0 = B^0 = 0, read only by the first iteration
+            continue;
+        }
+        a.dd[c] = scratch.floats(d.n);
+        if (!a.dd[c]) return scratch.status();
+        CILREG_CUDA(cudaMemsetAsync(a.dd[c], 0, sizeof(float) * d.n, s));
     }
     CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     // mu <- 1/mu, lambda = 2 mu (SB_TV_core.c:45-46)
@@ -162,9 +173,17 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
     a.f = f;
     int it = 0;
     if (T.use) {
-        // fused sweeps (U ping-pongs between u_out and u1), then the shrinkage
-        // and Bregman update of D, B in place from U2
+        // Iteration 0: both sweeps with the given D^0, B^0 (k_sb_sweep2).
+        // Iterations k >= 1: one pass forming D^k, B^k from U^k and B^{k-1}
+        // (k_sb_fused).  U ping-pongs between u_out and u1, B between the
+        // given buffers (B^0) and bb1.
         float* bufs[2] = {u_out, u1};
+        float* bb1[3] = {nullptr, nullptr, nullptr};
+        for (int c = 0; c < nc; c++) {
+            bb1[c] = scratch.floats(d.n);
+            if (!bb1[c]) return scratch.status();
+        }
+        float* const* bbuf[2] = {a.bb, bb1};
         SbSweepArgs w;
         for (int c = 0; c < 3; c++) {
             w.dd[c] = a.dd[c];
@@ -174,23 +193,51 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
         w.lambda = a.lambda;
         w.mu = a.mu;
         w.norm = a.norm;
-        a.check = 0;
+        SbFusedArgs z;
+        z.f = f;
+        z.lambda = a.lambda;
+        z.mu = a.mu;
+        z.norm = a.norm;
+        z.dlam = a.dlam;
         for (; it < iters; it++) {
             const int check = ctl.is_check(it) ? 1 : 0;
-            w.u = bufs[it & 1];
-            w.u2 = bufs[(it + 1) & 1];
-            CILREG_TRY(sb_sweep2_step(T, w, d, ctl.ctl(), check, ctl.partials(), s));
-            a.u = w.u2;
-            if (three) k_sb_shrink<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-            else k_sb_shrink<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, ctl.ctl());
-            CILREG_CUDA(cudaGetLastError());
-            note_launch(2);
+            if (it == 0) {
+                w.u = bufs[0];
+                w.u2 = bufs[1];
+                CILREG_TRY(sb_sweep2_step(T, w, d, ctl.ctl(), check, ctl.partials(), s));
+            } else {
+                z.u = bufs[it & 1];
+                z.u2 = bufs[(it + 1) & 1];
+                for (int c = 0; c < 3; c++) {
+                    z.bp[c] = bbuf[(it - 1) & 1][c];
+                    z.bn[c] = bbuf[it & 1][c];
+                }
+                CILREG_TRY(sb_fused_step(T, z, a.aniso != 0, d, ctl.ctl(), check, ctl.partials(), s));
+            }
+            note_launch();
             if (check) {
                 CILREG_TRY(ctl.after_check(it, nparts));
                 if (ctl.host_should_stop()) break;
             }
         }
         if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, bufs, u_out, d.n, s));
+        if (warm && iters > 0) {
+            // the warm state is D^n, B^n after the last iteration n - 1: bring
+            // B^{n-1} (written by iteration n - 1 into bbuf[(n - 1) & 1]) into
+            // warm->bb, then shrink once more from the final U, in place
+            for (int c = 0; c < nc; c++) {
+                float* pair[2] = {bb1[c], a.bb[c]};  // picks bbuf[last & 1]
+                CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, pair, a.bb[c], d.n, s));
+            }
+            StopCtl* never = (StopCtl*)scratch.bytes(sizeof(StopCtl));
+            if (!never) return scratch.status();
+            CILREG_CUDA(cudaMemsetAsync(never, 0, sizeof(StopCtl), s));
+            a.u = u_out;
+            if (three) k_sb_shrink<true><<<L.grid, L.block, 0, s>>>(a, d, L.kz, never);
+            else k_sb_shrink<false><<<L.grid, L.block, 0, s>>>(a, d, L.kz, never);
+            CILREG_CUDA(cudaGetLastError());
+            note_launch();
+        }
         return ctl.finish(info);
     }
     for (; it < iters; it++) {

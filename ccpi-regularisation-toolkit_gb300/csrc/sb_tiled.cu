@@ -196,6 +196,232 @@ __global__ void __launch_bounds__(NT, 2) k_sb_sweep2(SbSweepArgs a, Dims d, int 
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
+// shrinkage of v = grad U + B_prev into D, and the Bregman update B = v - D
+// (SB_TV_core.c:284-371): anisotropic per component, isotropic on |v|
+template <bool THREE, bool ANISO>
+__device__ __forceinline__ void sb_shrink(float g1, float g2, float g3, float b1, float b2, float b3, float dlam,
+                                          float& d1, float& d2, float& d3, float& n1, float& n2, float& n3) {
+    const float v1 = g1 + b1, v2 = g2 + b2, v3 = THREE ? g3 + b3 : 0.f;
+    if (ANISO) {
+        // (v / |v|) * max(|v| - 1/lambda, 0), 0 for v == 0: the same value as a sign copy
+        d1 = copysignf(fmaxf(fabsf(v1) - dlam, 0.f), v1);
+        d2 = copysignf(fmaxf(fabsf(v2) - dlam, 0.f), v2);
+        d3 = THREE ? copysignf(fmaxf(fabsf(v3) - dlam, 0.f), v3) : 0.f;
+    } else {
+        const float den = THREE ? sqrtf(v1 * v1 + v2 * v2 + v3 * v3) : sqrtf(v1 * v1 + v2 * v2);
+        const float m = fmaxf(den - dlam, 0.f);
+        const float r = (den != 0.f) ? __frcp_rn(den) : 0.f;  // v / den as v * (1/den), within 1 ulp
+        d1 = m * (v1 * r);
+        d2 = m * (v2 * r);
+        d3 = m * (v3 * r);
+    }
+    // B += (grad U) - D, summed as the reference does (SB_TV_core.c:366-368)
+    n1 = b1 + (g1 - d1);
+    n2 = b2 + (g2 - d2);
+    n3 = THREE ? b3 + (g3 - d3) : 0.f;
+}
+
+// One whole split-Bregman outer iteration k >= 1 in one streaming pass.  The
+// split variable is a function of the state: D^k = shrink(grad U^k + B^{k-1}),
+// B^k = B^{k-1} + grad U^k - D^k, so D is never stored; the pass reads U^k,
+// B^{k-1} and f, forms D^k and B^k on the fly, runs both Jacobi sweeps with
+// them and writes U^{k+1} and B^k (36 B per voxel in 3D, against 78 B for the
+// sweep pass plus a separate shrinkage pass).  Step j, with the tile and
+// halo of k_sb_sweep2 (D and B are needed one voxel further out, at i-1 and
+// j-1 of the sweep's halo, and need U one voxel beyond them at i+1, j+1):
+//   A0. forms D^k, B^k of plane j-1 (i/j successors of U^k from shared memory,
+//       k successor from registers); publishes Dx, Dy, Bx, By; writes B^k;
+//   A.  forms G and U1 of plane j-2 and publishes U1;
+//   B.  forms U2 of plane j-3 and writes it;
+//   C.  publishes U^k of plane j (loaded one step earlier).
+template <bool THREE, bool CHECK, bool ANISO>
+__global__ void __launch_bounds__(NT, 2) k_sb_fused(SbFusedArgs a, Dims d, int zc, const StopCtl* ctl,
+                                                    double2* partials) {
+    __shared__ float sU0[4][BY * BX];
+    __shared__ float sU1[2][BY * BX];
+    __shared__ float sDx[2][BY * BX];
+    __shared__ float sBx[2][BY * BX];
+    __shared__ float sDy[2][BY * BX];
+    __shared__ float sBy[2][BY * BX];
+    if (ctl->stop) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny, nz = d.nz;
+    const int x = blockIdx.x * OX + tx - 2;
+    const int y = blockIdx.y * OY + ty - 2;
+    const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
+    const bool o_pt = in_xy && tx >= 2 && tx <= BX - 3 && ty >= 2 && ty <= BY - 3;
+    int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
+    int xl = (nx == 1) ? tx : ((x - 1 < 0) ? tx + 1 : tx - 1);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    xh = min(max(xh, 0), BX - 1);
+    xl = min(max(xl, 0), BX - 1);
+    yh = min(max(yh, 0), BY - 1);
+    yl = min(max(yl, 0), BY - 1);
+    const int oc = ty * BX + tx;
+    const int oxh = ty * BX + xh, oxl = ty * BX + xl, oyh = yh * BX + tx, oyl = yl * BX + tx;
+    const int col = min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
+    const float lam = a.lambda, mu = a.mu, norm = a.norm, dlam = a.dlam;
+    float pa = 0.f, pb = 0.f;
+
+    if constexpr (!THREE) {
+        // one plane: D, B from U and B_prev; both sweeps (SB_TV_core.c:166-248)
+        const float u0 = __ldg(a.u + col), fv = __ldg(a.f + col);
+        sU0[0][oc] = u0;
+        __syncthreads();
+        float dx, dy, dz, bx, by, bz;
+        sb_shrink<false, ANISO>(sU0[0][oxh] - u0, sU0[0][oyh] - u0, 0.f, __ldg(a.bp[0] + col),
+                                __ldg(a.bp[1] + col), 0.f, dlam, dx, dy, dz, bx, by, bz);
+        if (o_pt) {
+            a.bn[0][col] = bx;
+            a.bn[1][col] = by;
+        }
+        sDx[0][oc] = dx;
+        sDy[0][oc] = dy;
+        sBx[0][oc] = bx;
+        sBy[0][oc] = by;
+        __syncthreads();
+        const float g = sDx[0][oxl] - dx + sDy[0][oyl] - dy - sBx[0][oxl] + bx - sBy[0][oyl] + by;
+        float s = g;
+        s += sU0[0][oxh] + sU0[0][oxl] + sU0[0][oyh] + sU0[0][oyl];
+        s *= lam;
+        s += mu * fv;
+        const float u1 = norm * s;
+        sU1[0][oc] = u1;
+        __syncthreads();
+        if (o_pt) {
+            float s2 = g;
+            s2 += sU1[0][oxh] + sU1[0][oxl] + sU1[0][oyh] + sU1[0][oyl];
+            s2 *= lam;
+            s2 += mu * fv;
+            const float u2 = norm * s2;
+            a.u2[col] = u2;
+            if (CHECK) {
+                const float df = u2 - u1;
+                pa = df * df;
+                pb = u2 * u2;
+            }
+        }
+    } else {
+        const int z0 = blockIdx.z * zc;
+        const int z1 = min(z0 + zc, nz);
+        const int sxy = (int)d.sxy;
+        auto at = [&](int k) -> int { return min(max(k, 0), nz - 1) * sxy + col; };
+        // registers entering step j: U^k of planes j, j-1, j-2, j-3; B^{k-1} of
+        // plane j-1; Dz, Bz of planes j-2, j-3; G of plane j-3; U1 of planes
+        // j-3, j-4
+        float cu = __ldg(a.u + at(z0 - 1)), pu = __ldg(a.u + at(z0 - 2)), ppu = __ldg(a.u + at(z0 - 3));
+        float pppu = 0.f;
+        float cb1 = __ldg(a.bp[0] + at(z0 - 2)), cb2 = __ldg(a.bp[1] + at(z0 - 2)), cb3 = __ldg(a.bp[2] + at(z0 - 2));
+        float dzb = 0.f, bzb = 0.f, dzc = 0.f, bzc = 0.f;
+        float gc = 0.f, u1c = 0.f, u1d = 0.f;
+        // f of planes j-1, j-2, j-3 entering step j = z0 - 1
+        float fa = __ldg(a.f + at(z0 - 2)), fb = __ldg(a.f + at(z0 - 3)), fc = 0.f;
+        // U ring slot of plane p: (p - z0 + 4) & 3; D/B and U1 slots: (p - z0 + 4) & 1
+        sU0[2][oc] = pu;  // plane z0-2
+        __syncthreads();
+
+        // R = (j - z0 + 1) & 3 for step j (steps start at j = z0 - 1)
+        auto step = [&](auto rr, auto full, int j) {
+            constexpr int R = decltype(rr)::value;
+            constexpr bool FULL = decltype(full)::value;
+            constexpr int SJ = (R + 3) & 3, SM1 = (R + 2) & 3, SM2 = (R + 1) & 3;  // U slots of j, j-1, j-2
+            constexpr int W1 = (R + 2) & 1, W2 = (R + 1) & 1, W3 = R & 1;         // parity slots of j-1, j-2, j-3
+            const int on = at(j + 1);
+            const float nu = __ldg(a.u + on);
+            const int ob = at(j);
+            const float nb1 = __ldg(a.bp[0] + ob), nb2 = __ldg(a.bp[1] + ob), nb3 = __ldg(a.bp[2] + ob);
+            const float nf = __ldg(a.f + ob);
+            // A0. D^k, B^k of plane m0 = j-1
+            float dx, dy, dza, bx, by, bza;
+            {
+                const int m0 = j - 1;
+                const float zhi = (m0 == nz - 1) ? ppu : cu;  // mirrored k+1 (SB_TV_core.c:293)
+                const float* U1s = sU0[SM1];
+                sb_shrink<true, ANISO>(U1s[oxh] - pu, U1s[oyh] - pu, zhi - pu, cb1, cb2, cb3, dlam, dx, dy, dza, bx,
+                                       by, bza);
+                if (o_pt && m0 >= z0 && m0 < z1) {
+                    const int v = m0 * sxy + col;
+                    a.bn[0][v] = bx;
+                    a.bn[1][v] = by;
+                    a.bn[2][v] = bza;
+                }
+                sDx[W1][oc] = dx;
+                sDy[W1][oc] = dy;
+                sBx[W1][oc] = bx;
+                sBy[W1][oc] = by;
+            }
+            // A. G and U1 of plane m = j-2 (SB_TV_core.c:273-280); its D, B were
+            // published in the previous step
+            const int m = j - 2;
+            const float dzl = (m == 0) ? dza : dzc;  // mirrored k-1
+            const float bzl = (m == 0) ? bza : bzc;
+            const float dval = sDx[W2][oxl] - sDx[W2][oc] + sDy[W2][oyl] - sDy[W2][oc] + dzl - dzb;
+            const float bval = -sBx[W2][oxl] + sBx[W2][oc] - sBy[W2][oyl] + sBy[W2][oc] - bzl + bzb;
+            const float g = dval + bval;
+            const float* Um = sU0[SM2];
+            const float zh0 = (m == nz - 1) ? pppu : pu, zl0 = (m == 0) ? pu : pppu;
+            float s = g;
+            s += Um[oxh] + Um[oxl] + Um[oyh] + Um[oyl] + zh0 + zl0;
+            s *= lam;
+            s += mu * fb;
+            const float u1 = norm * s;
+            sU1[W2][oc] = u1;
+            // B. U2 of plane kf = j-3
+            if (FULL) {
+                const int kf = j - 3;
+                const float zh1 = (kf == nz - 1) ? u1d : u1, zl1 = (kf == 0) ? u1 : u1d;
+                float s2 = gc;
+                s2 += sU1[W3][oxh] + sU1[W3][oxl] + sU1[W3][oyh] + sU1[W3][oyl] + zh1 + zl1;
+                s2 *= lam;
+                s2 += mu * fc;
+                const float u2 = norm * s2;
+                if (o_pt) a.u2[kf * sxy + col] = u2;
+                if (CHECK && o_pt) {
+                    const float df = u2 - u1c;
+                    pa += df * df;
+                    pb += u2 * u2;
+                }
+            }
+            // C. publish U^k of plane j
+            sU0[SJ][oc] = cu;
+            __syncthreads();
+            pppu = ppu;
+            ppu = pu;
+            pu = cu;
+            cu = nu;
+            cb1 = nb1;
+            cb2 = nb2;
+            cb3 = nb3;
+            dzc = dzb;
+            bzc = bzb;
+            dzb = dza;
+            bzb = bza;
+            gc = g;
+            u1d = u1c;
+            u1c = u1;
+            fc = fb;
+            fb = fa;
+            fa = nf;
+        };
+        step(Ic<0>{}, std::false_type{}, z0 - 1);
+        step(Ic<1>{}, std::false_type{}, z0);
+        step(Ic<2>{}, std::false_type{}, z0 + 1);
+        step(Ic<3>{}, std::false_type{}, z0 + 2);
+        int j = z0 + 3;
+        for (; j + 3 <= z1 + 2; j += 4) {
+            step(Ic<0>{}, std::true_type{}, j);
+            step(Ic<1>{}, std::true_type{}, j + 1);
+            step(Ic<2>{}, std::true_type{}, j + 2);
+            step(Ic<3>{}, std::true_type{}, j + 3);
+        }
+        if (j <= z1 + 2) step(Ic<0>{}, std::true_type{}, j);
+        if (j + 1 <= z1 + 2) step(Ic<1>{}, std::true_type{}, j + 1);
+        if (j + 2 <= z1 + 2) step(Ic<2>{}, std::true_type{}, j + 2);
+    }
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+}
+
 }  // namespace
 
 SbPlan sb_sweep2_plan(const Dims& d) {
@@ -222,6 +448,25 @@ int sb_sweep2_step(const SbPlan& T, const SbSweepArgs& a, const Dims& d, const S
     const bool three = d.nz > 1;
     auto kern = three ? (check ? k_sb_sweep2<true, true> : k_sb_sweep2<true, false>)
                       : (check ? k_sb_sweep2<false, true> : k_sb_sweep2<false, false>);
+    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+}  // namespace cilreg
+
+namespace cilreg {
+
+int sb_fused_step(const SbPlan& T, const SbFusedArgs& a, bool aniso, const Dims& d, const StopCtl* ctl, int check,
+                  double2* partials, cudaStream_t s) {
+    const bool three = d.nz > 1;
+    decltype(&k_sb_fused<true, true, true>) kern;
+    if (three)
+        kern = check ? (aniso ? k_sb_fused<true, true, true> : k_sb_fused<true, true, false>)
+                     : (aniso ? k_sb_fused<true, false, true> : k_sb_fused<true, false, false>);
+    else
+        kern = check ? (aniso ? k_sb_fused<false, true, true> : k_sb_fused<false, true, false>)
+                     : (aniso ? k_sb_fused<false, false, true> : k_sb_fused<false, false, false>);
     kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
     CILREG_CUDA(cudaGetLastError());
     return OK;

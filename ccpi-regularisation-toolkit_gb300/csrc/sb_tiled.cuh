@@ -15,6 +15,17 @@ struct SbSweepArgs {
     float lambda, mu, norm;
 };
 
+// one whole outer iteration k >= 1 (k_sb_fused): D^k and B^k formed on the
+// fly from U^k and B^{k-1}; writes U^{k+1} and B^k
+struct SbFusedArgs {
+    const float* u;        // U^k
+    float* u2;             // U^{k+1}
+    const float* f;
+    const float* bp[3];    // B^{k-1}
+    float* bn[3];          // B^k (distinct buffers: a neighbouring tile still reads B^{k-1})
+    float lambda, mu, norm, dlam;
+};
+
 struct SbPlan {
     dim3 grid, block;
     long long nblocks = 0;
@@ -27,5 +38,9 @@ SbPlan sb_sweep2_plan(const Dims& d);
 // per CTA (SbPlan::nblocks of them)
 int sb_sweep2_step(const SbPlan& T, const SbSweepArgs& a, const Dims& d, const StopCtl* ctl, int check,
                    double2* partials, cudaStream_t s);
+// one outer iteration k >= 1 with the shrinkage fused in (same tiling and
+// partial slots as sb_sweep2_step)
+int sb_fused_step(const SbPlan& T, const SbFusedArgs& a, bool aniso, const Dims& d, const StopCtl* ctl, int check,
+                  double2* partials, cudaStream_t s);
 
 }  // namespace cilreg

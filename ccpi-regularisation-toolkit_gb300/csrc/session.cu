@@ -36,7 +36,11 @@ int held_arrays(int alg, bool three) {
         default: return 5;                // previous output + x, y, z, xn
     }
 }
-int transient_arrays(int alg) { return alg == ALG_FGP ? 1 : 2; }
+int transient_arrays(int alg, bool three) {
+    if (alg == ALG_FGP) return 1;
+    if (alg == ALG_SB) return 1 + (three ? 3 : 2);  // U ping-pong + B ping-pong
+    return 2;
+}
 
 __global__ void k_grad_step(float* __restrict__ z, const float* __restrict__ y, const float* __restrict__ f,
                             float step, long long n) {
@@ -114,7 +118,7 @@ extern "C" {
 long long cilreg_prox_session_bytes(int alg, int dimX, int dimY, int dimZ) {
     if (check_dims(dimX, dimY, dimZ) != 0 || alg < 0 || alg > 3) return -1;
     const Dims d = make_dims(dimX, dimY, dimZ < 1 ? 1 : dimZ);
-    return (long long)(arr_bytes(d) * (size_t)(held_arrays(alg, d.nz > 1) + transient_arrays(alg))) + (1 << 20);
+    return (long long)(arr_bytes(d) * (size_t)(held_arrays(alg, d.nz > 1) + transient_arrays(alg, d.nz > 1))) + (1 << 20);
 }
 
 int cilreg_prox_session_create(cilreg_session** out, int alg, const float* params, int nparams, int dimX, int dimY,
