@@ -96,6 +96,8 @@ for _lib in (cilreg, cilregcuda):
     _lib.cilreg_version.restype = ctypes.c_char_p
     _lib.cilreg_device_count.restype = ctypes.c_int
     _lib.cilreg_launch_count.restype = ctypes.c_longlong
+    _lib.cilreg_release_cached.argtypes = [_I]
+    _lib.cilreg_release_cached.restype = ctypes.c_int
     _lib.cilreg_prox_session_bytes.argtypes = [_I, _I, _I, _I]
     _lib.cilreg_prox_session_bytes.restype = ctypes.c_longlong
 
@@ -131,6 +133,13 @@ def launch_count() -> int:
     """Kernels launched so far by the library (both names share one counter only
     when loaded as one object; each loaded library counts its own launches)."""
     return int(cilregcuda.cilreg_launch_count()) + int(cilreg.cilreg_launch_count())
+
+
+def release_cached(gpu_device: int = 0) -> None:
+    """Wait for the device's work and hand back the scratch memory the library
+    keeps cached in the device's stream-ordered pool."""
+    for lib in (cilregcuda, cilreg):
+        check_status(lib.cilreg_release_cached(int(gpu_device)), lib)
 
 
 def loaded_libraries():

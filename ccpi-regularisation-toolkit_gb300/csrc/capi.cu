@@ -84,6 +84,8 @@ int cilreg_device_count(void) {
     return n;
 }
 
+int cilreg_release_cached(int gpu_device) { return release_cached(gpu_device); }
+
 // ---------------------------------------------------------------------------
 // device-pointer API
 int cilreg_rof_tv_dev(const float* d_in, float* d_out, float* infovector, const float* d_lambda, float lambdaPar,

@@ -14,7 +14,8 @@
 //      once per voxel; D1, D2 (ROF) and the x, y LLT terms go to shared
 //      memory, the z terms stay in registers;
 //   C. updates plane j-2 (terms summed in the reference's order).
-// HBM traffic: read U and f, write U (12 B per voxel).
+// HBM traffic: read U and f, write U (12 B per voxel).  Element offsets are
+// 32-bit below 2^31 voxels, 64-bit from there.
 #include <math.h>
 #include <stdlib.h>
 
@@ -44,7 +45,7 @@ __device__ __forceinline__ float minmod_sq(float a, float b) {
 // sum is formed in float (the same denominator within an ulp)
 __device__ __forceinline__ float llt_term(float dxx) { return dxx / (fabsf(dxx) + 1.0e-12f); }
 
-template <bool THREE, bool CHECK>
+template <bool THREE, bool CHECK, class IT>
 __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                       const float* __restrict__ F, float lam_rof, float lam_llt,
                                                       float tau, Dims d, int zc, const StopCtl* ctl,
@@ -76,9 +77,9 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
     yl = min(max(yl, 0), BY - 1);
     const int oc = ty * BX + tx;
     const int oxh = ty * BX + xh, oxl = ty * BX + xl, oyh = yh * BX + tx, oyl = yl * BX + tx;
-    const int col = min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
-    const int sxy = (int)d.sxy;
-    auto at = [&](int k) -> int { return min(max(k, 0), nz - 1) * sxy + col; };
+    const IT col = (IT)min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
+    const IT sxy = (IT)d.sxy;
+    auto at = [&](int k) -> IT { return (IT)min(max(k, 0), nz - 1) * sxy + col; };
 
     // z registers: ROF D3 and the LLT z term of planes j-1 (a), j-2 (b), j-3 (c)
     float r3a = 0.f, r3b = 0.f, r3c = 0.f, l3a = 0.f, l3b = 0.f, l3c = 0.f;
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
             }
             const float u = sU[SM2][oc];
             const float un = u + tau * (lam_rof * div - lam_llt * laplc - (u - fa));
-            Un[kf * sxy + col] = un;
+            Un[(IT)kf * sxy + col] = un;
             if (CHECK) {
                 const float df = un - u;
                 pa += df * df;
@@ -186,7 +187,7 @@ LltPlan llt_plan(const Dims& d) {
     LltPlan T;
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
-        static const int resident = resident_ctas(k_llt_stream<true, false>, NT);
+        static const int resident = resident_ctas(k_llt_stream<true, false, int>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
         T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
     } else {
@@ -201,8 +202,6 @@ LltPlan llt_plan(const Dims& d) {
 
 int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
-    if (d.n >= (1LL << 31))
-        return fail(ERR_ARG, __FILE__, __LINE__, "LLT-ROF supports volumes below 2^31 voxels (got %lld)", d.n);
     Scratch scratch(s);
     const LltPlan T = llt_plan(d);
     IterControl ctl(s, scratch, iters, epsil, T.nblocks);
@@ -215,8 +214,13 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
-        auto kern = three ? (check ? k_llt_stream<true, true> : k_llt_stream<true, false>)
-                          : (check ? k_llt_stream<false, true> : k_llt_stream<false, false>);
+        decltype(&k_llt_stream<true, true, int>) kern;
+        if (d.n < (1LL << 31))
+            kern = three ? (check ? k_llt_stream<true, true, int> : k_llt_stream<true, false, int>)
+                         : (check ? k_llt_stream<false, true, int> : k_llt_stream<false, false, int>);
+        else
+            kern = three ? (check ? k_llt_stream<true, true, long long> : k_llt_stream<true, false, long long>)
+                         : (check ? k_llt_stream<false, true, long long> : k_llt_stream<false, false, long long>);
         kern<<<T.grid, T.block, 0, s>>>(bufs[it & 1], bufs[(it + 1) & 1], f, lam_rof, lam_llt, tau, d, T.zchunk,
                                         ctl.ctl(), ctl.partials());
         CILREG_CUDA(cudaGetLastError());

@@ -58,6 +58,15 @@ int use_device(int dev) {
     return OK;
 }
 
+int release_cached(int dev) {
+    CILREG_TRY(use_device(dev));
+    CILREG_CUDA(cudaDeviceSynchronize());
+    cudaMemPool_t pool;
+    CILREG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    CILREG_CUDA(cudaMemPoolTrimTo(pool, 0));
+    return OK;
+}
+
 cudaStream_t thread_stream(int dev) {
     struct Streams {
         cudaStream_t s[64] = {};
@@ -120,8 +129,22 @@ void* Scratch::bytes(size_t n) {
         return nullptr;
     }
     void* p = nullptr;
-    cudaError_t e = cudaMallocAsync(&p, n < 64 ? 64 : n, stream_);
+    const size_t sz = n < 64 ? 64 : n;
+    cudaError_t e = cudaMallocAsync(&p, sz, stream_);
+    // the pool keeps freed scratch; when the device is full, hand the unused
+    // part back first (then also what this stream's earlier calls freed) and
+    // retry, so that other allocators on the device are not starved by it
+    for (int attempt = 0; e == cudaErrorMemoryAllocation && attempt < 2; attempt++) {
+        cudaGetLastError();
+        if (attempt == 1) cudaStreamSynchronize(stream_);
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+            cudaMemPoolTrimTo(pool, 0);
+        e = cudaMallocAsync(&p, sz, stream_);
+    }
     if (e != cudaSuccess) {
+        cudaGetLastError();
         status_ = fail(e == cudaErrorMemoryAllocation ? ERR_OOM : ERR_CUDA, __FILE__, __LINE__,
                        "scratch allocation of %zu bytes failed: %s", n, cudaGetErrorString(e));
         return nullptr;

@@ -45,6 +45,9 @@ const char* last_error();
 // select the device (checks that one exists) and prepare its memory pool
 int use_device(int dev);
 
+// wait for the device's work, then return the memory its pool holds unused
+int release_cached(int dev);
+
 // a non-blocking stream owned by the calling host thread for device `dev`
 cudaStream_t thread_stream(int dev);
 

@@ -245,6 +245,13 @@ const char *cilreg_version(void);
 int cilreg_device_count(void);
 /* number of kernels this library has launched in the process so far */
 long long cilreg_launch_count(void);
+/* Scratch memory is taken from the device's stream-ordered pool and kept
+ * there when a call returns, so that later calls do not map it again; a call
+ * that finds the device full first hands the pool's unused memory back and
+ * retries.  This waits for all work on the device, then hands back what the
+ * pool holds unused (for callers that share the device with another
+ * allocator).  0 or a negative status. */
+int cilreg_release_cached(int gpu_device);
 
 #ifdef __cplusplus
 }
