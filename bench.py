@@ -364,7 +364,7 @@ def autograd_bench(args):
         y = fgp_tv(fr, lam, iters, 0, 1, ckpt, batched=True)
         loss = 0.5 * ((y - g) ** 2).sum()
         loss.backward()
-        return float(loss), float(lam.grad)
+        return float(loss.detach()), float(lam.grad)
 
     step()
     times = []
@@ -380,6 +380,33 @@ def autograd_bench(args):
     t = min(times)
     nvox = f.numel()
     print(json.dumps({"autograd": "FGP_TV 3D 8 x 128^3, 200 iterations, checkpoint 20, forward + adjoint",
+                      "seconds_per_step": t, "volumes_per_s": 8 / t,
+                      "forward_voxel_iters_per_s_equivalent": nvox * iters / t, "loss": loss, "dloss_dlambda": lg}))
+
+    # the same for unrolled ROF-TV (lambda 0.02, tau 0.001)
+    from ccpi.filters.autograd import rof_tv
+
+    def rof_step():
+        fr = f.clone().requires_grad_(True)
+        lam = torch.tensor(0.02, dtype=torch.float64, requires_grad=True)
+        y = rof_tv(fr, lam, iters, 0.001, ckpt, batched=True)
+        loss = 0.5 * ((y - g) ** 2).sum()
+        loss.backward()
+        return float(loss.detach()), float(lam.grad)
+
+    rof_step()
+    times = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        loss, lg = rof_step()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b) / 1e3)
+    t = min(times)
+    print(json.dumps({"autograd": "ROF_TV 3D 8 x 128^3, 200 iterations, tau 0.001, checkpoint 20, forward + adjoint",
                       "seconds_per_step": t, "volumes_per_s": 8 / t,
                       "forward_voxel_iters_per_s_equivalent": nvox * iters / t, "loss": loss, "dloss_dlambda": lg}))
     return 0

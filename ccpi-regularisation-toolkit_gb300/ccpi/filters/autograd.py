@@ -1,11 +1,12 @@
-"""Differentiable FGP-TV for torch: ``fgp_tv(f, lam, iterations)``.
+"""Differentiable FGP-TV and ROF-TV for torch: ``fgp_tv(f, lam, iterations)``
+and ``rof_tv(f, lam, iterations, tau)``.
 
 The forward pass is the production GPU iteration (no stopping rule); the
 backward pass is the library's hand-written adjoint of the unrolled
-iterations (``cilreg_fgp_tv_vjp_dev``), which stores the forward states every
-``checkpoint`` iterations and recomputes each segment before its reverse
-sweep.  Gradients flow to the input volume(s) and to the regularisation
-parameter, so lambda can be learned.
+iterations (``cilreg_fgp_tv_vjp_dev`` / ``cilreg_rof_tv_vjp_dev``), which
+stores the forward states every ``checkpoint`` iterations and recomputes each
+segment before its reverse sweep.  Gradients flow to the input volume(s) and
+to the regularisation parameter, so lambda can be learned.
 
 ``f`` is a float32 CUDA tensor of shape (Y, X), (Z, Y, X) or a batch
 (B, Z, Y, X) / (B, Y, X) when ``batched=True``; ``lam`` is a float or a
@@ -92,3 +93,76 @@ def fgp_tv(f, lam, iterations, methodTV=0, nonneg=0, checkpoint=20, batched=Fals
     if not torch.is_tensor(lam):
         lam = torch.tensor(float(lam), dtype=torch.float64)
     return FGPTVFunction.apply(f, lam, int(iterations), int(methodTV), int(nonneg), int(checkpoint), bool(batched))
+
+
+def _rof_forward_one(f, lam, iters, tau):
+    out = torch.empty_like(f)
+    info = (ctypes.c_float * 2)()
+    st = cilregcuda.cilreg_rof_tv_dev(f.data_ptr(), out.data_ptr(), info, None, float(lam), int(iters), float(tau),
+                                      0.0, *_dims(tuple(f.shape)), torch.cuda.current_stream(f.device).cuda_stream)
+    check_status(st)
+    return out
+
+
+def _rof_vjp_one(f, ybar, lam, iters, tau, ckpt):
+    fbar = torch.empty_like(f)
+    lb = ctypes.c_double(0.0)
+    st = cilregcuda.cilreg_rof_tv_vjp_dev(f.data_ptr(), ybar.data_ptr(), fbar.data_ptr(), ctypes.byref(lb),
+                                          float(lam), int(iters), float(tau), int(ckpt), *_dims(tuple(f.shape)),
+                                          torch.cuda.current_stream(f.device).cuda_stream)
+    check_status(st)
+    return fbar, lb.value
+
+
+def _per_volume_lams(lam, nvol):
+    lam_t = torch.as_tensor(lam, dtype=torch.float64).reshape(-1)
+    lams = lam_t.expand(nvol) if lam_t.numel() == 1 else lam_t
+    if lams.numel() != nvol:
+        raise ValueError("lam must be a scalar or hold one value per volume")
+    return lams.tolist()
+
+
+def _lam_grad(lbars, lam_shape):
+    if len(lam_shape) == 0 or (len(lbars) > 1 and int(torch.tensor(lam_shape).prod()) == 1):
+        return torch.tensor(sum(lbars), dtype=torch.float64).reshape(lam_shape)
+    return torch.tensor(lbars, dtype=torch.float64).reshape(lam_shape)
+
+
+class ROFTVFunction(torch.autograd.Function):
+    """y = ROF_TV(f, lam) unrolled for a fixed number of iterations (scalar lambda per volume)."""
+
+    @staticmethod
+    def forward(ctx, f, lam, iterations, tau, checkpoint, batched):
+        if not (f.is_cuda and f.dtype == torch.float32):
+            raise TypeError("f must be a float32 CUDA tensor")
+        f = f.contiguous()
+        vols = list(f) if batched else [f]
+        lams = _per_volume_lams(lam, len(vols))
+        outs = [_rof_forward_one(v, l, iterations, tau) for v, l in zip(vols, lams)]
+        ctx.save_for_backward(f)
+        ctx.lams = lams
+        ctx.lam_shape = torch.as_tensor(lam).shape
+        ctx.cfg = (iterations, tau, checkpoint, batched)
+        return torch.stack(outs) if batched else outs[0]
+
+    @staticmethod
+    def backward(ctx, ybar):
+        (f,) = ctx.saved_tensors
+        iterations, tau, ckpt, batched = ctx.cfg
+        ybar = ybar.contiguous()
+        vols = list(f) if batched else [f]
+        ybars = list(ybar) if batched else [ybar]
+        fbars, lbars = [], []
+        for v, yb, lam in zip(vols, ybars, ctx.lams):
+            fb, lb = _rof_vjp_one(v, yb, lam, iterations, tau, ckpt)
+            fbars.append(fb)
+            lbars.append(lb)
+        fbar = torch.stack(fbars) if batched else fbars[0]
+        return fbar, _lam_grad(lbars, ctx.lam_shape), None, None, None, None
+
+
+def rof_tv(f, lam, iterations, tau, checkpoint=20, batched=False):
+    """Differentiable unrolled ROF-TV (gradients w.r.t. ``f`` and ``lam``)."""
+    if not torch.is_tensor(lam):
+        lam = torch.tensor(float(lam), dtype=torch.float64)
+    return ROFTVFunction.apply(f, lam, int(iterations), float(tau), int(checkpoint), bool(batched))

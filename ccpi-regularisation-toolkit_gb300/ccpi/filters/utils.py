@@ -73,6 +73,7 @@ _PP = ctypes.POINTER(ctypes.c_void_p)
 _IP = ctypes.POINTER(ctypes.c_int)
 _VJP_SIGS = {
     "cilreg_fgp_tv_vjp_dev": [_V, _V, _V, ctypes.POINTER(ctypes.c_double), _F, _I, _I, _I, _I, _I, _I, _I, _V],
+    "cilreg_rof_tv_vjp_dev": [_V, _V, _V, ctypes.POINTER(ctypes.c_double), _F, _I, _F, _I, _I, _I, _I, _V],
 }
 _SESSION_SIGS = {
     "cilreg_prox_session_create": [ctypes.POINTER(ctypes.c_void_p), _I, _P, _I, _I, _I, _I, _V],

@@ -196,6 +196,13 @@ int cilreg_tgv_batch_dev(int nvol, const float *const *d_in, float *const *d_out
 int cilreg_fgp_tv_vjp_dev(const float *d_in, const float *d_ybar, float *d_inbar, double *lambar, float lambdaPar,
                           int iters, int methodTV, int nonneg, int checkpoint, int dimX, int dimY, int dimZ,
                           void *stream);
+/* The same for the unrolled ROF-TV map y = ROF(f, lambda) with scalar lambda,
+ * time step tau and `iters` iterations (the map cilreg_rof_tv_dev computes with
+ * d_lambda = NULL and epsil = 0); `checkpoint` >= 1 iterations per segment
+ * (one stored volume per segment plus checkpoint - 1 for the recomputed
+ * segment). */
+int cilreg_rof_tv_vjp_dev(const float *d_in, const float *d_ybar, float *d_inbar, double *lambar, float lambdaPar,
+                          int iters, float tau, int checkpoint, int dimX, int dimY, int dimZ, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Prox sessions (no counterpart in the reference, which discards all state at
