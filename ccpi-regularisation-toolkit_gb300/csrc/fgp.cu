@@ -116,7 +116,12 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     const TiledPlan T = fgp_tiled_plan(d);
     IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
     CILREG_TRY(ctl.status());
-    float* ring[3][3] = {};
+    // P^j lives in ring[j mod R]: R = 3 for single iterations (P^k overwrites
+    // P^{k-3}); R = 4 when iterations run in pairs, whose second output P^{k+1}
+    // must not overwrite the P^{k-2} that neighbouring tiles still read
+    const PairPlan TP = (T.use && !warm) ? fgp_pair_plan(d) : PairPlan{};
+    const int R = TP.use ? 4 : 3;
+    float* ring[4][3] = {};
     int base = 0;
     if (warm) {
         // warm start: the caller's dual buffers hold P_{-1}, P_{-2} of this call
@@ -124,27 +129,52 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         for (int r = 0; r < 3; r++)
             for (int c = 0; c < 3; c++) ring[r][c] = warm->ring[(base + r) % 3][c];
     } else {
-        for (int r = 0; r < 3; r++)
+        for (int r = 0; r < R; r++)
             for (int c = 0; c < nc; c++) {
                 ring[r][c] = scratch.floats(d.n);
                 if (!ring[r][c]) return scratch.status();
             }
         // P^{-1} = P^{-2} = 0 (the reference's calloc'd P, P_prev, R)
-        for (int r = 1; r < 3; r++)
+        for (int r = R - 2; r < R; r++)
             for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(ring[r][c], 0, sizeof(float) * d.n, s));
     }
 
     const float multip = three ? (1.0f / (12.0f * lam)) : (1.0f / (8.0f * lam));
     float tk = 1.0f;   // t_{k}
     float cprev = 0.0f;  // c_{k-1}; R^{(0)} = 0 whatever its value
+    auto writes_u = [&](int k) {
+        return (k == iters - 1) || ctl.is_check(k) || (ctl.checking() && ((k + 1) % 5 == 0));
+    };
+    auto writes_p = [&](int k) { return (k != iters - 1) || warm != nullptr; };
     int it = 0;
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
+        if (TP.use && it + 1 < iters && !check && !ctl.is_check(it + 1) && !writes_u(it) && writes_p(it)) {
+            // iterations it and it+1 in one pass
+            const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;
+            const float cnext = (tk - 1.0f) / tkp1;
+            float* pn1[3] = {ring[it % R][0], ring[it % R][1], ring[it % R][2]};
+            float* pn2[3] = {ring[(it + 1) % R][0], ring[(it + 1) % R][1], ring[(it + 1) % R][2]};
+            const float* pc[3] = {ring[(it + R - 1) % R][0], ring[(it + R - 1) % R][1], ring[(it + R - 1) % R][2]};
+            const float* po[3] = {ring[(it + R - 2) % R][0], ring[(it + R - 2) % R][1], ring[(it + R - 2) % R][2]};
+            CILREG_TRY(fgp_pair_step(TP, pc, po, pn1, pn2, f, u_out, lam, cprev, cnext, multip, nonneg == 1,
+                                     methodTV != 0, writes_u(it + 1) ? 1 : 0, writes_p(it + 1) ? 1 : 0, d, ctl.ctl(),
+                                     s));
+            note_launch();
+            // advance the momentum sequence by two iterations (FGP_TV_core.c:138-139)
+            tk = tkp1;
+            cprev = cnext;
+            const float tkp2 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;
+            cprev = (tk - 1.0f) / tkp2;
+            tk = tkp2;
+            it++;
+            continue;
+        }
         FgpArgs a;
         for (int c = 0; c < 3; c++) {
-            a.pn[c] = ring[it % 3][c];
-            a.pc[c] = ring[(it + 2) % 3][c];
-            a.po[c] = ring[(it + 1) % 3][c];
+            a.pn[c] = ring[it % R][c];
+            a.pc[c] = ring[(it + R - 1) % R][c];
+            a.po[c] = ring[(it + R - 2) % R][c];
         }
         a.f = f;
         a.u = u_out;
@@ -154,8 +184,8 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         a.nonneg = (nonneg == 1);
         a.aniso = (methodTV != 0);
         a.check = check;
-        a.write_u = (it == iters - 1) || check || (ctl.checking() && ((it + 1) % 5 == 0));
-        a.write_p = (it != iters - 1) || warm;  // a warm state keeps the last dual iterate
+        a.write_u = writes_u(it);
+        a.write_p = writes_p(it);  // a warm state keeps the last dual iterate
         if (T.use)
             CILREG_TRY(fgp_tiled_step(T, a.pc, a.po, a.pn, f, u_out, lam, cprev, multip, a.nonneg, a.aniso,
                                       a.write_u, a.write_p, check, d, ctl.ctl(), ctl.partials(), s));

@@ -22,6 +22,22 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
                    const float* const* b = nullptr);
 
+// Two iterations k, k+1 in one streaming pass (fgp_pair.cu; 3D only).
+struct PairPlan {
+    bool use = false;  // CILREG_FGP_PAIR=1 turns pairs on
+    dim3 grid, block;
+    long long nblocks = 0;
+    int zchunk = 0;
+};
+PairPlan fgp_pair_plan(const Dims& d);
+// reads P^{k-1} (pc), P^{k-2} (po) and f, writes P^k (pn1) and P^{k+1} (pn2,
+// when write_p2) and U^{k+1} (when write_u2); c1, c2: the momentum
+// coefficients of iterations k and k+1.  No stopping check.
+int fgp_pair_step(const PairPlan& T, const float* const pc[3], const float* const po[3], float* const pn1[3],
+                  float* const pn2[3], const float* f, float* u, float lam, float c1, float c2, float multip,
+                  int nonneg, int aniso, int write_u2, int write_p2, const Dims& d, const StopCtl* ctl,
+                  cudaStream_t s);
+
 // One volume of a batched FGP run (device-resident descriptor table).
 struct FgpBatchVol {
     Dims d;

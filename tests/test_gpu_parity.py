@@ -216,6 +216,26 @@ def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(2, 30, 31), (3, 29, 15), (10, 16, 22), (67, 70, 9), (130, 33, 35), (65, 57, 29),
+                                   (200, 41, 60)], ids=str)
+def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
+    """Two iterations per streaming pass (temporal blocking) give the same
+    iterates as one iteration per pass: same arithmetic, bit for bit, and the
+    same stopping iteration."""
+    from ccpi.filters.regularisers import FGP_TV
+
+    rng = np.random.default_rng(7 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil, iters in ((0, 1, 3e-4, 80), (1, 0, 0.0, 37), (0, 0, 0.0, 2), (0, 1, 1e-2, 41)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        monkeypatch.setenv("CILREG_FGP_PAIR", "1")
+        a = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ia)
+        monkeypatch.delenv("CILREG_FGP_PAIR")
+        b = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ib)
+        assert int(ia[0]) == int(ib[0])
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
                                    (130, 33, 35), (151, 12, 31)], ids=str)
 def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
