@@ -185,6 +185,15 @@ def run_reference(args):
     return 0
 
 
+def fgp_kernel_name(nx):
+    """The 3D FGP iteration kernel the library runs for an x extent of nx: the
+    tensor-copy-staged kernel when the row pitch allows it, else the
+    thread-loading one."""
+    if nx % 4 == 0 and os.environ.get("CILREG_FGP_TMA", "1") != "0":
+        return "FGP iteration (k_fgp_tma, csrc/fgp_tma.cu)"
+    return "FGP iteration (k_fgp_stream, csrc/fgp_tiled.cu)"
+
+
 def profile_case(args):
     """Device-only FGP calls with a fixed iteration count: the small, repeatable
     command the committed ncu summaries were captured from."""
@@ -654,7 +663,7 @@ def main():
     tpv = _ncu_traffic_per_voxel()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": (tpv * n if tpv is not None else None), "peak_kind": peak_kind,
-                "kernel": "FGP iteration (k_fgp_stream, csrc/fgp_tiled.cu)", "launch_ms": per_launch * 1e3,
+                "kernel": fgp_kernel_name(nx), "launch_ms": per_launch * 1e3,
                 "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_ITER * n}
 
     # end to end through the reference-facing C ABI with pinned host buffers

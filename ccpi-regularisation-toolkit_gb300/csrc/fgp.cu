@@ -11,6 +11,8 @@
 // 40 B per voxel-iteration in 3D (28 B in 2D).  U_k is written to the output
 // only on iterations that need it (the last one, stopping checks, and the
 // iteration before a check, whose U is the check's U_prev).
+#include <vector>
+
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
 
@@ -113,14 +115,17 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
-    const TiledPlan T = fgp_tiled_plan(d);
-    IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
-    CILREG_TRY(ctl.status());
+    TiledPlan T = fgp_tiled_plan(d);
     // P^j lives in ring[j mod R]: R = 3 for single iterations (P^k overwrites
     // P^{k-3}); R = 4 when iterations run in pairs, whose second output P^{k+1}
     // must not overwrite the P^{k-2} that neighbouring tiles still read
     const PairPlan TP = (T.use && !warm) ? fgp_pair_plan(d) : PairPlan{};
     const int R = TP.use ? 4 : 3;
+    // the tensor-copy kernel: same tiles, z chunks balanced for its own occupancy
+    bool tma = T.use && !TP.use && fgp_tma_usable(d);
+    if (tma) T = fgp_tiled_plan(d, fgp_tma_resident());
+    IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
+    CILREG_TRY(ctl.status());
     float* ring[4][3] = {};
     int base = 0;
     if (warm) {
@@ -137,6 +142,19 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         // P^{-1} = P^{-2} = 0 (the reference's calloc'd P, P_prev, R)
         for (int r = R - 2; r < R; r++)
             for (int c = 0; c < nc; c++) CILREG_CUDA(cudaMemsetAsync(ring[r][c], 0, sizeof(float) * d.n, s));
+    }
+
+    // tensor maps of (P^{k-1}, P^{k-2}, f) for each position of the ring
+    std::vector<unsigned char> maps;
+    if (tma) {
+        const size_t mb = fgp_tma_maps_bytes();
+        maps.resize(mb * R);
+        for (int r = 0; r < R && tma; r++) {
+            const float* arr[8] = {ring[(r + R - 1) % R][0], ring[(r + R - 1) % R][1], ring[(r + R - 1) % R][2],
+                                   ring[(r + R - 2) % R][0], ring[(r + R - 2) % R][1], ring[(r + R - 2) % R][2],
+                                   f, u_out};
+            tma = fgp_tma_encode(arr, d, maps.data() + mb * r);
+        }
     }
 
     const float multip = three ? (1.0f / (12.0f * lam)) : (1.0f / (8.0f * lam));
@@ -186,7 +204,10 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         a.check = check;
         a.write_u = writes_u(it);
         a.write_p = writes_p(it);  // a warm state keeps the last dual iterate
-        if (T.use)
+        if (tma)
+            CILREG_TRY(fgp_tma_step(T, maps.data() + fgp_tma_maps_bytes() * (it % R), a.pn, u_out, lam, cprev, multip,
+                                    a.nonneg, a.aniso, a.write_u, a.write_p, check, d, ctl.ctl(), ctl.partials(), s));
+        else if (T.use)
             CILREG_TRY(fgp_tiled_step(T, a.pc, a.po, a.pn, f, u_out, lam, cprev, multip, a.nonneg, a.aniso,
                                       a.write_u, a.write_p, check, d, ctl.ctl(), ctl.partials(), s));
         else if (three)
@@ -206,6 +227,7 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     }
     StopCtl done;
     CILREG_TRY(ctl.finish(info, &done));
+    if (tma) CILREG_TRY(fgp_tma_status(s));
     if (warm) {
         // iterations 0..last wrote ring[(base + it) % 3]
         const int ran = done.stop ? done.iters + 1 : iters;

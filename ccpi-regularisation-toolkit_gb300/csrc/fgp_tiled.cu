@@ -259,7 +259,7 @@ int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long n
 
 int fgp_default_zchunk(const Dims& d) { return (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1; }
 
-TiledPlan fgp_tiled_plan(const Dims& d) {
+TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm) {
     TiledPlan T;
     const char* e = getenv("CILREG_FGP_KERNEL");
     T.use = !(e && e[0] == 's');  // "simple" selects the per-voxel kernel of fgp.cu
@@ -269,7 +269,7 @@ TiledPlan fgp_tiled_plan(const Dims& d) {
         // many volumes and keeps fgp_default_zchunk)
         static const int resident = resident_ctas(k_fgp_stream<true, false, int>, NT);
         const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
-        T.zchunk = wave_zchunk(tiles, d.nz, resident, 2, ZCHUNK);
+        T.zchunk = wave_zchunk(tiles, d.nz, resident_ctas_per_sm > 0 ? resident_ctas_per_sm : resident, 2, ZCHUNK);
     } else {
         T.zchunk = 1;
     }

@@ -12,7 +12,8 @@ struct TiledPlan {
     int zchunk = 0;
 };
 
-TiledPlan fgp_tiled_plan(const Dims& d);
+// z chunks balanced for `resident_ctas_per_sm` CTAs per SM (0: those of k_fgp_stream)
+TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm = 0);
 int fgp_default_zchunk(const Dims& d);
 
 // one FGP iteration; with `b` (three device arrays, the unit gradient field
@@ -37,6 +38,23 @@ int fgp_pair_step(const PairPlan& T, const float* const pc[3], const float* cons
                   float* const pn2[3], const float* f, float* u, float lam, float c1, float c2, float multip,
                   int nonneg, int aniso, int write_u2, int write_p2, const Dims& d, const StopCtl* ctl,
                   cudaStream_t s);
+
+// The iteration with tensor-copy (TMA) staging of its inputs (fgp_tma.cu):
+// 3D, x extent a multiple of 4, below 2^31 voxels; CILREG_FGP_TMA=0 turns it off.
+bool fgp_tma_usable(const Dims& d);
+// tensor maps of the eight inputs (pc[0..2], po[0..2], f, U) into `maps_out`
+// (fgp_tma_maps_bytes() bytes); false when an array is not 16-byte aligned or
+// the driver refuses the map
+bool fgp_tma_encode(const float* const arrays[8], const Dims& d, void* maps_out);
+size_t fgp_tma_maps_bytes();
+// CTAs of the tensor-copy kernel resident per SM
+int fgp_tma_resident();
+// same contract as fgp_tiled_step, inputs given by the tensor maps
+int fgp_tma_step(const TiledPlan& T, const void* maps, float* const pn[3], float* u, float lam, float c,
+                 float multip, int nonneg, int aniso, int write_u, int write_p, int check, const Dims& d,
+                 const StopCtl* ctl, double2* partials, cudaStream_t s);
+// after a run: fails if a tensor-copy wait timed out (synchronises `s`)
+int fgp_tma_status(cudaStream_t s);
 
 // One volume of a batched FGP run (device-resident descriptor table).
 struct FgpBatchVol {

@@ -216,6 +216,26 @@ def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(2, 30, 32), (3, 29, 16), (10, 16, 24), (67, 70, 12), (130, 33, 36), (65, 57, 28),
+                                   (200, 41, 60), (33, 100, 4)], ids=str)
+def test_fgp_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
+    """The iteration whose inputs are staged by tensor copies (x extent a
+    multiple of 4) gives the iterates of the thread-loading kernel bit for bit,
+    and the same stopping iteration."""
+    from ccpi.filters.regularisers import FGP_TV
+
+    rng = np.random.default_rng(11 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil, iters in ((0, 1, 3e-4, 80), (1, 0, 0.0, 37), (0, 0, 0.0, 1), (0, 1, 1e-2, 41)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_FGP_TMA", "0")
+        b = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_FGP_TMA")
+        assert int(ia[0]) == int(ib[0])
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("shape", [(2, 30, 31), (3, 29, 15), (10, 16, 22), (67, 70, 9), (130, 33, 35), (65, 57, 29),
                                    (200, 41, 60)], ids=str)
 def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
