@@ -15,6 +15,7 @@ to the regularisation parameter, so lambda can be learned.
 from __future__ import annotations
 
 import ctypes
+from concurrent.futures import ThreadPoolExecutor
 
 import torch
 
@@ -38,14 +39,36 @@ def _forward_one(f, lam, iters, method, nonneg):
     return out
 
 
-def _vjp_one(f, ybar, lam, iters, method, nonneg, ckpt):
-    fbar = torch.empty_like(f)
+def _vjp_one(f, ybar, lam, iters, method, nonneg, ckpt, fbar):
     lb = ctypes.c_double(0.0)
     st = cilregcuda.cilreg_fgp_tv_vjp_dev(f.data_ptr(), ybar.data_ptr(), fbar.data_ptr(), ctypes.byref(lb),
                                           float(lam), int(iters), int(method), int(nonneg), int(ckpt),
                                           *_dims(tuple(f.shape)), torch.cuda.current_stream(f.device).cuda_stream)
     check_status(st)
-    return fbar, lb.value
+    return lb.value
+
+
+def _parallel(vjp, vols, ybars, lams):
+    """Run one vector-Jacobian product per volume, concurrently: each volume on
+    its own host thread and CUDA stream (the library call releases the GIL and
+    returns once its stream is done), so small volumes fill the GPU together.
+    Outputs are allocated on the caller's stream before the workers start."""
+    fbars = [torch.empty_like(v) for v in vols]
+    if len(vols) == 1:
+        return fbars, [vjp(vols[0], ybars[0], lams[0], fbars[0])]
+    caller = torch.cuda.current_stream(vols[0].device)
+    ready = torch.cuda.Event()
+    ready.record(caller)
+
+    def work(i):
+        s = torch.cuda.Stream(device=vols[i].device)
+        s.wait_event(ready)
+        with torch.cuda.stream(s):
+            return vjp(vols[i], ybars[i], lams[i], fbars[i])
+
+    with ThreadPoolExecutor(max_workers=len(vols)) as ex:
+        lbars = list(ex.map(work, range(len(vols))))
+    return fbars, lbars
 
 
 class FGPTVFunction(torch.autograd.Function):
@@ -61,7 +84,13 @@ class FGPTVFunction(torch.autograd.Function):
         lams = lam_t.expand(len(vols)) if lam_t.numel() == 1 else lam_t
         if lams.numel() != len(vols):
             raise ValueError("lam must be a scalar or hold one value per volume")
-        outs = [_forward_one(v, float(l), iterations, methodTV, nonneg) for v, l in zip(vols, lams.tolist())]
+        if len(vols) > 1:
+            # all volumes in one batched run (one graph launch, bit-equal to single calls)
+            from .batch import FGP_TV_batch
+
+            outs = FGP_TV_batch(vols, lams.tolist(), iterations, 0.0, methodTV, nonneg, f.device.index or 0)
+        else:
+            outs = [_forward_one(v, float(l), iterations, methodTV, nonneg) for v, l in zip(vols, lams.tolist())]
         ctx.save_for_backward(f)
         ctx.lams = lams.tolist()
         ctx.lam_shape = torch.as_tensor(lam).shape
@@ -75,11 +104,8 @@ class FGPTVFunction(torch.autograd.Function):
         ybar = ybar.contiguous()
         vols = list(f) if batched else [f]
         ybars = list(ybar) if batched else [ybar]
-        fbars, lbars = [], []
-        for v, yb, lam in zip(vols, ybars, ctx.lams):
-            fb, lb = _vjp_one(v, yb, lam, iterations, method, nonneg, ckpt)
-            fbars.append(fb)
-            lbars.append(lb)
+        fbars, lbars = _parallel(lambda v, yb, lam, fb: _vjp_one(v, yb, lam, iterations, method, nonneg, ckpt, fb),
+                                 vols, ybars, ctx.lams)
         fbar = torch.stack(fbars) if batched else fbars[0]
         if len(ctx.lam_shape) == 0 or (len(lbars) > 1 and int(torch.tensor(ctx.lam_shape).prod()) == 1):
             lam_bar = torch.tensor(sum(lbars), dtype=torch.float64).reshape(ctx.lam_shape)
@@ -104,14 +130,13 @@ def _rof_forward_one(f, lam, iters, tau):
     return out
 
 
-def _rof_vjp_one(f, ybar, lam, iters, tau, ckpt):
-    fbar = torch.empty_like(f)
+def _rof_vjp_one(f, ybar, lam, iters, tau, ckpt, fbar):
     lb = ctypes.c_double(0.0)
     st = cilregcuda.cilreg_rof_tv_vjp_dev(f.data_ptr(), ybar.data_ptr(), fbar.data_ptr(), ctypes.byref(lb),
                                           float(lam), int(iters), float(tau), int(ckpt), *_dims(tuple(f.shape)),
                                           torch.cuda.current_stream(f.device).cuda_stream)
     check_status(st)
-    return fbar, lb.value
+    return lb.value
 
 
 def _per_volume_lams(lam, nvol):
@@ -152,11 +177,8 @@ class ROFTVFunction(torch.autograd.Function):
         ybar = ybar.contiguous()
         vols = list(f) if batched else [f]
         ybars = list(ybar) if batched else [ybar]
-        fbars, lbars = [], []
-        for v, yb, lam in zip(vols, ybars, ctx.lams):
-            fb, lb = _rof_vjp_one(v, yb, lam, iterations, tau, ckpt)
-            fbars.append(fb)
-            lbars.append(lb)
+        fbars, lbars = _parallel(lambda v, yb, lam, fb: _rof_vjp_one(v, yb, lam, iterations, tau, ckpt, fb),
+                                 vols, ybars, ctx.lams)
         fbar = torch.stack(fbars) if batched else fbars[0]
         return fbar, _lam_grad(lbars, ctx.lam_shape), None, None, None, None
 
