@@ -124,3 +124,21 @@ def test_invalid_arguments_raise():
         FGP_dTV(x, np.zeros((9, 8), np.float32), 0.05, 10, 0.0, 0.2, 0, 0, device="gpu")
     with pytest.raises(ValueError):
         TV_ENERGY(x, x, 0.1, 3)
+
+
+@pytest.mark.parametrize("shape", [(300, 300, 300), (97, 512, 515)], ids=str)
+def test_large_host_arrays_match_the_device_call(shape):
+    """Host-pointer calls on volumes of 100-500 MB (pageable arrays in, a
+    fresh or caller-given output array out) return exactly the device-pointer
+    call's result."""
+    import torch
+    from ccpi.filters import regularisersCuPy as D
+    from ccpi.filters.regularisers import FGP_TV, ROF_TV
+
+    rng = np.random.default_rng(sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    ref = D.FGP_TV(torch.from_numpy(x).cuda(), 0.05, 6, 0.0, 0, 1).cpu().numpy()
+    np.testing.assert_array_equal(FGP_TV(x, 0.05, 6, 0.0, 0, 1, device="gpu"), ref)
+    out = np.empty_like(x)
+    ROF_TV(x, 0.02, 5, 0.001, 0.0, device="gpu", out=out)
+    np.testing.assert_array_equal(out, D.ROF_TV(torch.from_numpy(x).cuda(), 0.02, 5, 0.001).cpu().numpy())
