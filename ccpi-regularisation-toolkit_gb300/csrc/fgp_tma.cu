@@ -16,20 +16,21 @@
 // or past the end) arrive as zeros, which is the zero boundary the
 // iteration needs.  Waits on an mbarrier are bounded: one that runs out sets
 // an error flag that the host turns into a failed call.
-#include <cuda.h>
 #include <stdint.h>
 #include <stdlib.h>
 
 #include "fgp_tiled.cuh"
+#include "tma_ring.cuh"
 
 namespace cilreg {
 
 namespace {
 
+using namespace tma;
+
 constexpr int BX = 32, BY = 16;          // threads
 constexpr int OX = BX - 2, OY = BY - 2;  // output voxels per tile
 constexpr int NT = BX * BY;
-constexpr int BOXX = 36;                 // box width (floats): 32 + up to 3 for the alignment
 constexpr int BOX = BOXX * BY;           // floats per array per stage
 constexpr int NIN = 8;                   // pc (3), po (3), f, and U_prev on check iterations
 // arrays staged (7, or 8 on check iterations) and ring depth (planes in
@@ -40,7 +41,6 @@ struct Ring {
     static constexpr int STAGES = ST;
     static constexpr size_t DYN = sizeof(float) * BOX * NA * STAGES + 128;  // + alignment slack
 };
-constexpr long long WAIT_LIMIT = 1LL << 20;  // tries of a suspending wait: about a second
 
 __device__ int g_tma_timeout = 0;
 
@@ -54,32 +54,6 @@ struct TmaArgs {
 struct TmaMaps {
     CUtensorMap m[NIN];  // pc[0..2], po[0..2], f, U
 };
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ void tma_load(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];\n" ::"r"(smem_addr(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-        : "memory");
-}
 
 template <bool CHECK, int ST>
 __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMaps maps, TmaArgs a, Dims d, int zc,
@@ -98,7 +72,7 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
     const int nx = d.nx, ny = d.ny, nz = d.nz;
     const int xf = blockIdx.x * OX - 1;  // x of thread tx = 0
     const int yf = blockIdx.y * OY - 1;
-    const int bx0 = xf - (((xf % 4) + 4) % 4);  // box origin: xf rounded down to a multiple of 4
+    const int bx0 = box_x0(xf);
     const int rx = xf - bx0;
     const int x = xf + tx, y = yf + ty;
     const int z0 = blockIdx.z * zc;
@@ -114,14 +88,14 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
 
     if (leader) {
         for (int s = 0; s < STAGES; s++) mbar_init(&bar[s]);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        mbar_init_fence();
     }
     __syncthreads();
     auto issue = [&](int p) {  // plane z0-1+p into stage p % STAGES
         const int s = p % STAGES;
         float* dst = stage0 + (size_t)s * BOX * NA;
         mbar_expect(&bar[s], STAGE_BYTES);
-        for (int q = 0; q < NA; q++) tma_load(dst + q * BOX, &maps.m[q], bx0, yf, z0 - 1 + p, &bar[s]);
+        for (int q = 0; q < NA; q++) load_box(dst + q * BOX, &maps.m[q], bx0, yf, z0 - 1 + p, &bar[s]);
     };
     if (leader)
         for (int p = 0; p < STAGES - 1 && p < nplanes; p++) issue(p);
@@ -133,15 +107,9 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
     for (int k = z0 - 1; k <= z1; ++k) {
         const int p = k - (z0 - 1);
         // wait for plane k's stage (bounded), read this voxel's inputs
-        {
-            const int s = p % STAGES;
-            const uint32_t parity = (uint32_t)((p / STAGES) & 1);
-            bool ok = dead;
-            for (long long t = 0; !ok && t < WAIT_LIMIT; t++) ok = mbar_try(&bar[s], parity);
-            if (!ok) {
-                atomicExch(&g_tma_timeout, 1);
-                dead = true;
-            }
+        if (!dead && !wait_stage(&bar[p % STAGES], p / STAGES)) {
+            atomicExch(&g_tma_timeout, 1);
+            dead = true;
         }
         const float* st = stage0 + (size_t)(p % STAGES) * BOX * NA + own;
         const float c1 = st[0 * BOX], c2 = st[1 * BOX], c3 = st[2 * BOX];
@@ -158,7 +126,7 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
         __syncthreads();
         // every thread has read plane k-1's stage: refill it with plane k+STAGES-1
         if (leader && p + STAGES - 1 < nplanes) {
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            proxy_fence();
             issue(p + STAGES - 1);
         }
         // 2. U of plane k
@@ -213,47 +181,19 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
-using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeFn encoder() {
-    static EncodeFn fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            p = nullptr;
-        cudaGetLastError();
-        return (EncodeFn)p;
-    }();
-    return fn;
-}
-
 }  // namespace
 
 bool fgp_tma_usable(const Dims& d) {
     const char* e = getenv("CILREG_FGP_TMA");
     if (e && e[0] == '0') return false;
     // row stride (nx floats) must be a multiple of 16 bytes; 32-bit offsets
-    return d.nz > 1 && d.nx % 4 == 0 && d.n < (1LL << 31) && encoder() != nullptr;
+    return tma::volume_ok(d) && d.n < (1LL << 31);
 }
 
 bool fgp_tma_encode(const float* const arrays[8], const Dims& d, void* maps_out) {
     TmaMaps* M = (TmaMaps*)maps_out;
     for (int q = 0; q < NIN; q++)
-        if (((uintptr_t)arrays[q] & 15) != 0) return false;  // a tensor's base must be 16-byte aligned
-    const cuuint64_t dims[3] = {(cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
-    const cuuint64_t strides[2] = {(cuuint64_t)d.nx * sizeof(float), (cuuint64_t)d.sxy * sizeof(float)};
-    const cuuint32_t box[3] = {BOXX, BY, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    for (int q = 0; q < NIN; q++) {
-        const CUresult r = encoder()(&M->m[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)arrays[q], dims, strides,
-                                     box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return false;
-    }
+        if (!tma::encode(&M->m[q], arrays[q], d, BY)) return false;
     return true;
 }
 
