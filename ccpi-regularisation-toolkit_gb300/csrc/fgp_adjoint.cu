@@ -14,7 +14,8 @@
 //   fbar  += Zbar_k
 //   lambar += -<Zbar_k, A R_k> + (dm/dlambda) <Qbar_k, B U_k>
 //   Rbar_k = Qbar_k - lambda A^T Zbar_k,  (A^T Z)_c = Z - Z[+e_c] (0 past the last index)
-// Three kernels per reverse iteration (Qbar, Zbar, Rbar).  The forward states
+// Four kernels per reverse iteration: Z_k and A R_k once per voxel, then
+// Qbar, Zbar, Rbar.  The forward states
 // are stored every `ckpt` iterations and each segment is recomputed with the
 // production iteration kernel before its reverse sweep, so the linearisation
 // point is exactly the forward pass the caller saw.
@@ -40,6 +41,8 @@ struct AdjArgs {
     float* zb;            // Zbar_k (out of kernel b)
     float* fbar;          // accumulated
     float* rb0[3];        // Rbar_k (out of kernel c)
+    float* zz;            // Z_k = f - lambda A R_k (before the clamp; kernel u)
+    float* ar;            // A R_k (kernel u)
     float lam, m, ck, a1, a2;
     int nonneg, aniso;
 };
@@ -63,13 +66,6 @@ __device__ __forceinline__ float ar_at(const AdjArgs& a, const Dims& d, int i, i
     return r_at<THREE>(a, 0, v) + r_at<THREE>(a, 1, v) - b1 - b2;
 }
 
-template <bool THREE>
-__device__ __forceinline__ float u_at(const AdjArgs& a, const Dims& d, int i, int j, int k) {
-    float u = ldg(a.f, vid(d, i, j, k)) - a.lam * ar_at<THREE>(a, d, i, j, k);
-    if (a.nonneg && u < 0.f) u = 0.f;
-    return u;
-}
-
 #define ADJ_LOOP_BEGIN                                       \
     const int i = blockIdx.x * 32 + threadIdx.x;             \
     const int j = blockIdx.y * 8 + threadIdx.y;              \
@@ -85,15 +81,29 @@ __device__ __forceinline__ float u_at(const AdjArgs& a, const Dims& d, int i, in
     }                \
     }
 
+// u: Z_k = f - lambda A R_k (the objective step before the clamp) and A R_k,
+// once per voxel (same expressions as u_at)
+template <bool THREE>
+__global__ void __launch_bounds__(256) k_adj_u(AdjArgs a, Dims d, int kz) {
+    ADJ_LOOP_BEGIN
+    const float ar = ar_at<THREE>(a, d, i, j, k);
+    a.ar[v] = ar;
+    a.zz[v] = ldg(a.f, v) - a.lam * ar;
+    ADJ_LOOP_END
+    (void)acc;
+}
+
+__device__ __forceinline__ float clamp_u(const AdjArgs& a, float z) { return (a.nonneg && z < 0.f) ? 0.f : z; }
+
 // a: Qbar_k = J^T Pbar_k, and <Qbar_k, B U_k> into the partials
 template <bool THREE>
 __global__ void __launch_bounds__(256) k_adj_q(AdjArgs a, Dims d, int kz, double2* partials) {
     ADJ_LOOP_BEGIN
-    const float u = u_at<THREE>(a, d, i, j, k);
+    const float u = clamp_u(a, ldg(a.zz, v));
     float bu[3] = {0.f, 0.f, 0.f};
-    bu[0] = (i == d.nx - 1) ? 0.f : u - u_at<THREE>(a, d, i + 1, j, k);
-    bu[1] = (j == d.ny - 1) ? 0.f : u - u_at<THREE>(a, d, i, j + 1, k);
-    if (THREE) bu[2] = (k == d.nz - 1) ? 0.f : u - u_at<THREE>(a, d, i, j, k + 1);
+    bu[0] = (i == d.nx - 1) ? 0.f : u - clamp_u(a, ldg(a.zz, v + 1));
+    bu[1] = (j == d.ny - 1) ? 0.f : u - clamp_u(a, ldg(a.zz, v + d.nx));
+    if (THREE) bu[2] = (k == d.nz - 1) ? 0.f : u - clamp_u(a, ldg(a.zz, v + d.sxy));
     const int nc = THREE ? 3 : 2;
     float q[3], pb[3], qb[3];
     for (int c = 0; c < 3; c++) {
@@ -133,8 +143,8 @@ __global__ void __launch_bounds__(256) k_adj_z(AdjArgs a, Dims d, int kz, double
     if (THREE) w += ((k < d.nz - 1) ? ldg(a.qb[2], v) : 0.f) - ((k >= 1) ? ldg(a.qb[2], v - d.sxy) : 0.f);
     w = a.m * w;
     if (a.ybar) w += ldg(a.ybar, v);
-    const float ar = ar_at<THREE>(a, d, i, j, k);
-    const float z = ldg(a.f, v) - a.lam * ar;
+    const float ar = ldg(a.ar, v);
+    const float z = ldg(a.zz, v);
     const float zb = (a.nonneg && z < 0.f) ? 0.f : w;
     a.zb[v] = zb;
     a.fbar[v] += zb;
@@ -224,11 +234,13 @@ int fgp_vjp_run(const float* f, const float* ybar, float lam, int iters, int met
         if (!qb[c]) return sc.status();
     }
     float* zb = arr(n);
+    float* zz = arr(n);
+    float* arv = arr(n);
     StopCtl* ctl = (StopCtl*)sc.bytes(sizeof(StopCtl));
     double* acc = (double*)sc.bytes(2 * sizeof(double));
     const Launch3 LA = plan_launch(d);
     double2* part = (double2*)sc.bytes(sizeof(double2) * (size_t)num_blocks(LA));
-    if (!zb || !ctl || !acc || !part) return sc.status();
+    if (!zb || !zz || !arv || !ctl || !acc || !part) return sc.status();
     CILREG_TRY(launch_init_ctl(ctl, iters, s));
     CILREG_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
     CILREG_CUDA(cudaMemsetAsync(fbar, 0, sizeof(float) * n, s));
@@ -299,6 +311,8 @@ int fgp_vjp_run(const float* f, const float* ybar, float lam, int iters, int met
             a.f = f;
             a.ybar = (k == L - 1) ? ybar : nullptr;
             a.zb = zb;
+            a.zz = zz;
+            a.ar = arv;
             a.fbar = fbar;
             a.lam = lam;
             a.m = m;
@@ -308,12 +322,14 @@ int fgp_vjp_run(const float* f, const float* ybar, float lam, int iters, int met
             a.nonneg = (nonneg == 1);
             a.aniso = (methodTV != 0);
             if (three) {
+                k_adj_u<true><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz);
                 k_adj_q<true><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz, part);
                 k_accumulate<<<1, 1024, 0, s>>>(part, num_blocks(LA), acc, 0);
                 k_adj_z<true><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz, part);
                 k_accumulate<<<1, 1024, 0, s>>>(part, num_blocks(LA), acc, 1);
                 k_adj_r<true><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz);
             } else {
+                k_adj_u<false><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz);
                 k_adj_q<false><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz, part);
                 k_accumulate<<<1, 1024, 0, s>>>(part, num_blocks(LA), acc, 0);
                 k_adj_z<false><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz, part);
@@ -321,7 +337,7 @@ int fgp_vjp_run(const float* f, const float* ybar, float lam, int iters, int met
                 k_adj_r<false><<<LA.grid, LA.block, 0, s>>>(a, d, LA.kz);
             }
             CILREG_CUDA(cudaGetLastError());
-            note_launch(5);
+            note_launch(6);
         }
     }
     double h[2] = {0.0, 0.0};
