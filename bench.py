@@ -189,7 +189,8 @@ def fgp_kernel_name(nx):
     """The 3D FGP iteration kernel the library runs for an x extent of nx: the
     tensor-copy-staged kernel when the row pitch allows it, else the
     thread-loading one."""
-    if nx % 4 == 0 and os.environ.get("CILREG_FGP_TMA", "1") != "0":
+    e = os.environ.get("CILREG_FGP_TMA", "")
+    if nx % 4 == 0 and e != "0" and (e == "1" or nx ** 3 >= 2 ** 25):
         return "FGP iteration (k_fgp_tma, csrc/fgp_tma.cu)"
     return "FGP iteration (k_fgp_stream, csrc/fgp_tiled.cu)"
 

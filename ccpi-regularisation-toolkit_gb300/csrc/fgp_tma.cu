@@ -187,7 +187,10 @@ bool fgp_tma_usable(const Dims& d) {
     const char* e = getenv("CILREG_FGP_TMA");
     if (e && e[0] == '0') return false;
     // row stride (nx floats) must be a multiple of 16 bytes; 32-bit offsets
-    return tma::volume_ok(d) && d.n < (1LL << 31);
+    // below about 32 M voxels (256^3: 2.25 waves of CTAs) the thread-loading
+    // kernel is as fast or faster; the staging pays off on large volumes
+    const long long min_n = (e && e[0] == '1') ? 0 : (1LL << 25);
+    return tma::volume_ok(d) && d.n >= min_n && d.n < (1LL << 31);
 }
 
 bool fgp_tma_encode(const float* const arrays[8], const Dims& d, void* maps_out) {

@@ -228,6 +228,7 @@ def test_fgp_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
     x = rng.random(shape).astype(np.float32)
     for method, nonneg, epsil, iters in ((0, 1, 3e-4, 80), (1, 0, 0.0, 37), (0, 0, 0.0, 1), (0, 1, 1e-2, 41)):
         ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        monkeypatch.setenv("CILREG_FGP_TMA", "1")  # staging at any size (by default from 2^25 voxels)
         a = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ia)
         monkeypatch.setenv("CILREG_FGP_TMA", "0")
         b = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ib)
