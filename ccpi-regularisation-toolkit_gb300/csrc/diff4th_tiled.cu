@@ -12,7 +12,9 @@
 //   C. updates plane j-2 from W of planes j-3, j-2, j-1 (z from registers,
 //      x/y from shared memory).
 // One barrier per plane.  HBM traffic: read U and f, write U (12 B/voxel);
-// the reference's two sweeps move 24 B and store W.
+// the reference's two sweeps move 24 B and store W.  The kernel is bound by
+// instruction issue and latency: at 40 registers three CTAs fit on an SM
+// (1.41 -> 1.31 ms per 512^3 iteration against two CTAs at 56 registers).
 #include <type_traits>
 
 #include "diff4th_tiled.cuh"
@@ -32,7 +34,7 @@ using Ic = std::integral_constant<int, V>;
 // CHECK: a stopping-check iteration (per-CTA partial sums).  IT: element-offset
 // type (int below 2^31 voxels).
 template <bool THREE, bool CHECK, typename IT>
-__global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
+__global__ void __launch_bounds__(NT, 3) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                      const float* __restrict__ F, float lam, float tau, float isg2,
                                                      Dims d, int zc, const StopCtl* ctl, double2* partials) {
     __shared__ float sU[4][BY][BX];

@@ -14,7 +14,9 @@
 //      once per voxel; D1, D2 (ROF) and the x, y LLT terms go to shared
 //      memory, the z terms stay in registers;
 //   C. updates plane j-2 (terms summed in the reference's order).
-// HBM traffic: read U and f, write U (12 B per voxel).  Element offsets are
+// HBM traffic: read U and f, write U (12 B per voxel).  Two CTAs per SM at
+// about 60 registers: limited to 40 registers for three, the 3D variants
+// spill and run slower (1.25 -> 1.30 ms per 512^3 iteration).  Element offsets are
 // 32-bit below 2^31 voxels, 64-bit from there.
 #include <math.h>
 #include <stdlib.h>
