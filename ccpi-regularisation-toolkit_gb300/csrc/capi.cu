@@ -168,12 +168,15 @@ int TV_FGP_GPU_main(float* Input, float* Output, float* infovector, float lambda
                     int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ) {
     CILREG_TRY(check_dims(dimX, dimY, dimZ));
     const Dims d = dims_of(dimX, dimY, dimZ);
-    // FGP never copies Input into Output: with a stopping rule the caller's
-    // Output is U_prev of iteration 0 (FGP_TV_core.c:66,123)
-    return host_call(Input, Output, gpu_device, d, epsil != 0.0f || iter <= 0,
-                     [&](const float* di, float* dout, cudaStream_t s) {
-                         return fgp_run(di, dout, lambdaPar, iter, epsil, methodTV, nonneg, d, s, infovector);
-                     });
+    // U_prev of iteration 0: the C-OMP path takes the caller's Output
+    // (FGP_TV_core.c:66,123, zeros from the Python layer); the reference GPU
+    // path copies its uninitialised device U instead (TV_FGP_GPU_core.cu:377,
+    // 516).  Here it is zero on the device, so the caller's Output is not
+    // uploaded (it is, unchanged, when no iteration runs).
+    return host_call(Input, Output, gpu_device, d, iter <= 0, [&](const float* di, float* dout, cudaStream_t s) {
+        if (epsil != 0.0f && iter > 0) CILREG_CUDA(cudaMemsetAsync(dout, 0, sizeof(float) * d.n, s));
+        return fgp_run(di, dout, lambdaPar, iter, epsil, methodTV, nonneg, d, s, infovector);
+    });
 }
 
 int TV_PD_GPU_main(float* Input, float* Output, float* infovector, float lambdaPar, int iter, float epsil,
@@ -236,9 +239,12 @@ int dTV_FGP_GPU_main(float* Input, float* InputRef, float* Output, float* infove
     CILREG_TRY(check_dims(dimX, dimY, dimZ));
     if (!InputRef) return fail(ERR_ARG, __FILE__, __LINE__, "null InputRef pointer");
     const Dims d = dims_of(dimX, dimY, dimZ);
-    // as FGP: with a stopping rule the caller's Output is U_prev of iteration 0
-    return host_call(Input, Output, gpu_device, d, epsil != 0.0f || iter <= 0,
+    // as FGP: U_prev of iteration 0 is zero on the device (dTV_FGP_GPU_core.cu
+    // leaves it uninitialised; the C-OMP path takes the caller's Output)
+    return host_call(Input, Output, gpu_device, d, iter <= 0,
                      [&](const float* di, float* dout, cudaStream_t s) {
+                         if (epsil != 0.0f && iter > 0)
+                             CILREG_CUDA(cudaMemsetAsync(dout, 0, sizeof(float) * d.n, s));
                          Scratch sc(s);
                          float* dr = sc.floats(d.n);
                          if (!dr) return sc.status();

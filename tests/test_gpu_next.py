@@ -142,3 +142,28 @@ def test_large_host_arrays_match_the_device_call(shape):
     out = np.empty_like(x)
     ROF_TV(x, 0.02, 5, 0.001, 0.0, device="gpu", out=out)
     np.testing.assert_array_equal(out, D.ROF_TV(torch.from_numpy(x).cuda(), 0.02, 5, 0.001).cpu().numpy())
+
+
+def test_gpu_entry_points_start_u_prev_at_zero():
+    """TV_FGP_GPU_main / dTV_FGP_GPU_main with a stopping rule take U_prev of
+    iteration 0 as zero on the device (the reference GPU path leaves it
+    uninitialised): whatever the caller's Output holds, the result and the
+    stopping iteration are those of the C-OMP call with a zero Output."""
+    from ccpi.filters.TV import TV_FGP_GPU, dTV_FGP_GPU
+    from ccpi.filters.regularisers import FGP_TV, FGP_dTV
+
+    rng = np.random.default_rng(5)
+    x = rng.random((20, 24, 28)).astype(np.float32)
+    r = rng.random((20, 24, 28)).astype(np.float32)
+    ref_info = np.zeros(2, np.float32)
+    ref = FGP_TV(x, 0.05, 60, 1e-3, 0, 1, device="cpu", infovector=ref_info)
+    info = np.zeros(2, np.float32)
+    got = TV_FGP_GPU(x, 0.05, 60, 1e-3, 0, 1, 0, out=rng.random(x.shape).astype(np.float32), infovector=info)
+    np.testing.assert_array_equal(got, ref)
+    assert int(info[0]) == int(ref_info[0])
+    ref_info = np.zeros(2, np.float32)
+    ref = FGP_dTV(x, r, 0.05, 60, 1e-3, 0.2, 0, 1, device="cpu", infovector=ref_info)
+    got = dTV_FGP_GPU(x, r, 0.05, 60, 1e-3, 0.2, 0, 1, 0, out=rng.random(x.shape).astype(np.float32),
+                      infovector=info)
+    np.testing.assert_array_equal(got, ref)
+    assert int(info[0]) == int(ref_info[0])
