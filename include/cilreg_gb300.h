@@ -39,7 +39,9 @@ int TV_ROF_GPU_main(float *Input, float *Output, float *infovector, float lambda
                     float epsil, int gpu_device, int N, int M, int Z);
 
 /* replaces TV_FGP_GPU_main, src/Core/regularisers_GPU/TV_FGP_GPU_core.h:7.
- * As in the CPU reference, Output's initial content is U_prev of iteration 0. */
+ * U_prev of iteration 0 is zero (the reference GPU path leaves it
+ * uninitialised; TV_FGP_CPU_main takes Output's initial content, as the CPU
+ * reference does); Output is only written. */
 int TV_FGP_GPU_main(float *Input, float *Output, float *infovector, float lambdaPar, int iter, float epsil,
                     int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ);
 
@@ -74,7 +76,7 @@ int LLT_ROF_GPU_main(float *Input, float *Output, float *infovector, float lambd
                      int iterationsNumb, float tau, float epsil, int gpu_device, int N, int M, int Z);
 
 /* replaces dTV_FGP_GPU_main, src/Core/regularisers_GPU/dTV_FGP_GPU_core.h:7.
- * As in the CPU reference, Output's initial content is U_prev of iteration 0. */
+ * U_prev of iteration 0 is zero, as in TV_FGP_GPU_main. */
 int dTV_FGP_GPU_main(float *Input, float *InputRef, float *Output, float *infovector, float lambdaPar, int iter,
                      float epsil, float eta, int methodTV, int nonneg, int gpu_device, int dimX, int dimY, int dimZ);
 
