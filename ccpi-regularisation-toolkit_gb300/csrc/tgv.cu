@@ -314,6 +314,72 @@ int tgv_batch_step(const TgvBatchVol* d_vols, const int* d_tile_vol, long long n
     return OK;
 }
 
+namespace {
+
+// 3D: one fused pass per iteration over double-buffered U, V, P, Q
+int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2,
+                  float epsil, const Dims& d, cudaStream_t s, float* info, const TgvPlan& T, Scratch& scratch) {
+    IterControl ctl(s, scratch, iters, epsil, T.nblocks);
+    CILREG_TRY(ctl.status());
+    const size_t nb = sizeof(float) * (size_t)d.n;
+    float* ub[2] = {u_out, scratch.floats(d.n)};
+    float* vb[2][3] = {};
+    float* pb[2][3] = {};
+    float* qb[2][6] = {};
+    if (!ub[1]) return scratch.status();
+    for (int b = 0; b < 2; b++) {
+        for (int c = 0; c < 3; c++) {
+            vb[b][c] = scratch.floats(d.n);
+            pb[b][c] = scratch.floats(d.n);
+            if (!vb[b][c] || !pb[b][c]) return scratch.status();
+        }
+        for (int c = 0; c < 6; c++)
+            if (!(qb[b][c] = scratch.floats(d.n))) return scratch.status();
+    }
+    // the initial state: U = U0, V = P = Q = 0 (calloc, TGV_core.c:57-70, 128-133)
+    for (int c = 0; c < 3; c++) {
+        CILREG_CUDA(cudaMemsetAsync(vb[0][c], 0, nb, s));
+        CILREG_CUDA(cudaMemsetAsync(pb[0][c], 0, nb, s));
+    }
+    for (int c = 0; c < 6; c++) CILREG_CUDA(cudaMemsetAsync(qb[0][c], 0, nb, s));
+    CILREG_CUDA(cudaMemcpyAsync(u_out, f, nb, cudaMemcpyDeviceToDevice, s));
+    TgvFusedArgs a;
+    a.u0 = f;
+    a.lambda = lam;
+    a.alpha1 = alpha1;
+    a.alpha0 = alpha0;
+    a.tau = (float)pow((double)L2, -0.5);  // TGV_core.c:54-55
+    a.sigma = a.tau;
+    a.inv_lt = 1.0f / (a.lambda + a.tau);
+    int it = 0;
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        const int cur = it & 1, nxt = cur ^ 1;
+        a.u = ub[cur];
+        a.un = ub[nxt];
+        for (int c = 0; c < 3; c++) {
+            a.v[c] = vb[cur][c];
+            a.vn[c] = vb[nxt][c];
+            a.p[c] = pb[cur][c];
+            a.pn[c] = pb[nxt][c];
+        }
+        for (int c = 0; c < 6; c++) {
+            a.q[c] = qb[cur][c];
+            a.qn[c] = qb[nxt][c];
+        }
+        CILREG_TRY(tgv_fused_step(T, a, d, ctl.ctl(), check, ctl.partials(), s));
+        note_launch();
+        if (check) {
+            CILREG_TRY(ctl.after_check(it, T.nblocks));
+            if (ctl.host_should_stop()) break;
+        }
+    }
+    if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, ub, u_out, d.n, s));
+    return ctl.finish(info);
+}
+
+}  // namespace
+
 int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
     const bool three = d.nz > 1;
@@ -321,6 +387,8 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);
     const TgvPlan T = tgv_primal_plan(d);
+    const TgvPlan TF = T.use ? tgv_fused_plan(d) : TgvPlan{};
+    if (TF.use) return tgv_run_fused(f, u_out, lam, alpha1, alpha0, iters, L2, epsil, d, s, info, TF, scratch);
     const long long nparts = T.use ? T.nblocks : num_blocks(L);
     IterControl ctl(s, scratch, iters, epsil, nparts);
     CILREG_TRY(ctl.status());

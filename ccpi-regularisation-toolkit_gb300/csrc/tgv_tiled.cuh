@@ -22,6 +22,25 @@ int tgv_dual_stream_step(const TgvPlan& T, const TgvArgs& a, const Dims& d, cons
 int tgv_dual_batch_step(const TgvBatchVol* d_vols, const int* d_ptile_vol, long long nptiles, bool three,
                         cudaStream_t s);
 
+// one whole iteration (dual and primal halves) in one pass over double-
+// buffered state (tgv_fused.cu; 3D, below 2^31 voxels; CILREG_TGV_FUSED=0
+// turns it off)
+struct TgvFusedArgs {
+    const float* u;   // extrapolated U (old)
+    const float* u0;
+    const float* v[3];
+    const float* p[3];
+    const float* q[6];
+    float* un;        // new
+    float* vn[3];
+    float* pn[3];
+    float* qn[6];
+    float lambda, alpha1, alpha0, tau, sigma, inv_lt;
+};
+TgvPlan tgv_fused_plan(const Dims& d);
+int tgv_fused_step(const TgvPlan& T, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl, int check,
+                   double2* partials, cudaStream_t s);
+
 // tiling of the streaming primal kernel in a batched run (64-plane chunks)
 void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);
 // primal half-iteration of every volume of a batch: one flat grid over the

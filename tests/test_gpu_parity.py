@@ -216,6 +216,26 @@ def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(2, 30, 31), (3, 29, 15), (10, 16, 22), (67, 70, 9), (130, 33, 35), (65, 57, 29),
+                                   (33, 100, 4), (9, 1, 40), (5, 40, 1)], ids=str)
+def test_tgv_fused_pass_equals_two_passes(shape, monkeypatch):
+    """One pass per TGV iteration over double-buffered state equals the dual
+    and primal streaming passes in place, bit for bit, with the same stopping
+    iteration."""
+    from ccpi.filters.regularisers import TGV
+
+    rng = np.random.default_rng(19 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil, iters in ((0.0, 37), (3e-3, 80), (0.0, 1)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = TGV(x, 0.05, 1.0, 2.0, iters, 12.0, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_TGV_FUSED", "0")
+        b = TGV(x, 0.05, 1.0, 2.0, iters, 12.0, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_TGV_FUSED")
+        assert int(ia[0]) == int(ib[0])
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("shape", [(2, 30, 32), (3, 29, 16), (10, 16, 24), (67, 70, 12), (130, 33, 36), (65, 57, 28),
                                    (200, 41, 60), (33, 100, 4)], ids=str)
 def test_fgp_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
