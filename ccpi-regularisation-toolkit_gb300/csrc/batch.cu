@@ -318,6 +318,117 @@ int fgp_batch_run(int nvol, const float* const* f, float* const* u, const int* d
 }
 
 // --------------------------------------------------------------------------
+// TGV batch, 3D: one fused pass per iteration (tgv_fused.cu) over every
+// volume's double-buffered state
+int tgv_batch_run_fused(int nvol, const float* const* f, float* const* u, const BatchLayout& L, const float* lams,
+                        float alpha1, float alpha0, int iters, float L2, float epsil, float* infos, cudaStream_t s) {
+    Scratch sc(s);
+    const float tau = (float)pow((double)L2, -0.5);  // TGV_core.c:54-55
+    std::vector<TgvFusedVol> vols(nvol);
+    long long ntiles = 0;
+    size_t state_floats = 0;
+    for (int v = 0; v < nvol; v++) {
+        TgvFusedVol& V = vols[v];
+        V.d = L.dims[v];
+        tgv_fused_tiles(V.d, V.gx, V.gy, V.gz, V.zc);
+        V.tile_base = ntiles;
+        ntiles += (long long)V.gx * V.gy * V.gz;
+        // two copies of V (3), P (3), Q (6) and a second U
+        state_floats += align256(sizeof(float) * (size_t)V.d.n) / sizeof(float) * (2 * 12 + 1);
+    }
+    if (ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "batch too large (%lld tiles)", ntiles);
+    float* state = (float*)sc.bytes(sizeof(float) * state_floats);
+    double2* part = (double2*)sc.bytes(sizeof(double2) * (size_t)ntiles);
+    StopCtl* d_ctl = (StopCtl*)sc.bytes(sizeof(StopCtl) * nvol);
+    TgvFusedVol* d_vols = (TgvFusedVol*)sc.bytes(sizeof(TgvFusedVol) * nvol);
+    int* d_tile_vol = (int*)sc.bytes(sizeof(int) * (size_t)ntiles);
+    CheckSlot* d_slots = (CheckSlot*)sc.bytes(sizeof(CheckSlot) * nvol);
+    StopCtl** d_ctlp = (StopCtl**)sc.bytes(sizeof(StopCtl*) * nvol);
+    if (!state || !part || !d_ctl || !d_vols || !d_tile_vol || !d_slots || !d_ctlp) return sc.status();
+    std::vector<int> tile_vol(ntiles);
+    std::vector<CheckSlot> slots(nvol);
+    std::vector<StopCtl*> ctlp(nvol);
+    std::vector<float*> ualt(nvol);
+    // zero V, P, Q of buffer 0 (the buffers of parity 1 are written before they are read)
+    float* r = state;
+    for (int v = 0; v < nvol; v++) {
+        TgvFusedVol& V = vols[v];
+        const size_t n = (size_t)V.d.n, stride = align256(sizeof(float) * n) / sizeof(float);
+        float* vb[2][3];
+        float* pb[2][3];
+        float* qb[2][6];
+        for (int b = 0; b < 2; b++) {
+            for (int c = 0; c < 3; c++) { vb[b][c] = r; r += stride; }
+            for (int c = 0; c < 3; c++) { pb[b][c] = r; r += stride; }
+            for (int c = 0; c < 6; c++) { qb[b][c] = r; r += stride; }
+        }
+        ualt[v] = r;
+        r += stride;
+        for (int c = 0; c < 3; c++) {
+            CILREG_CUDA(cudaMemsetAsync(vb[0][c], 0, sizeof(float) * n, s));
+            CILREG_CUDA(cudaMemsetAsync(pb[0][c], 0, sizeof(float) * n, s));
+        }
+        for (int c = 0; c < 6; c++) CILREG_CUDA(cudaMemsetAsync(qb[0][c], 0, sizeof(float) * n, s));
+        CILREG_CUDA(cudaMemcpyAsync(u[v], f[v], sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        float* ub[2] = {u[v], ualt[v]};
+        for (int par = 0; par < 2; par++) {
+            TgvFusedArgs& A = V.args[par];
+            const int cur = par, nxt = par ^ 1;
+            A.u = ub[cur];
+            A.un = ub[nxt];
+            A.u0 = f[v];
+            for (int c = 0; c < 3; c++) {
+                A.v[c] = vb[cur][c];
+                A.vn[c] = vb[nxt][c];
+                A.p[c] = pb[cur][c];
+                A.pn[c] = pb[nxt][c];
+            }
+            for (int c = 0; c < 6; c++) {
+                A.q[c] = qb[cur][c];
+                A.qn[c] = qb[nxt][c];
+            }
+            A.lambda = lams[v];
+            A.alpha1 = alpha1;
+            A.alpha0 = alpha0;
+            A.tau = tau;
+            A.sigma = tau;
+            A.inv_lt = 1.0f / (A.lambda + tau);
+        }
+        V.ctl = d_ctl + v;
+        V.partials = part + V.tile_base;
+        const long long nt = (long long)V.gx * V.gy * V.gz;
+        for (long long t = 0; t < nt; t++) tile_vol[V.tile_base + t] = v;
+        slots[v] = CheckSlot{V.partials, nt, V.ctl};
+        ctlp[v] = V.ctl;
+    }
+    CILREG_CUDA(cudaMemcpyAsync(d_vols, vols.data(), sizeof(TgvFusedVol) * nvol, cudaMemcpyHostToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(d_tile_vol, tile_vol.data(), sizeof(int) * (size_t)ntiles, cudaMemcpyHostToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(d_slots, slots.data(), sizeof(CheckSlot) * nvol, cudaMemcpyHostToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(d_ctlp, ctlp.data(), sizeof(StopCtl*) * nvol, cudaMemcpyHostToDevice, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    CILREG_TRY(launch_init_ctls(d_ctlp, nvol, iters, s));
+    auto enqueue = [&]() -> int {
+        for (int it = 0; it < iters; it++) {
+            const int check = (epsil != 0.0f && it % 5 == 0) ? 1 : 0;
+            CILREG_TRY(tgv_fused_batch_step(d_vols, d_tile_vol, ntiles, it & 1, check, s));
+            note_launch();
+            if (check) CILREG_TRY(launch_finalize_batch(d_slots, nvol, epsil, it, s));
+        }
+        return OK;
+    };
+    if (env_flag("CILREG_BATCH_GRAPH", true) && iters > 0)
+        CILREG_TRY(run_graph(s, enqueue));
+    else
+        CILREG_TRY(enqueue());
+    // the last iterate of each volume is in the buffer its last iteration wrote
+    for (int v = 0; v < nvol && iters > 0; v++) {
+        float* ub[2] = {u[v], ualt[v]};
+        CILREG_TRY(launch_select_pingpong(d_ctl + v, iters, ub, u[v], L.dims[v].n, s));
+    }
+    return read_infos(d_ctl, nvol, infos, s);
+}
+
+// --------------------------------------------------------------------------
 // TGV batch
 int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* dims, const float* lams, float alpha1,
                   float alpha0, int iters, float L2, float epsil, float* infos, cudaStream_t caller) {
@@ -341,6 +452,9 @@ int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* d
     bool stream_primal = !(ek && ek[0] == 's');
     for (int v = 0; v < nvol; v++)
         if (L.dims[v].n >= (1LL << 31)) stream_primal = false;
+    // 3D batches run the fused pass (CILREG_TGV_FUSED=0: the two passes)
+    if (L.three && stream_primal && env_flag("CILREG_TGV_FUSED", true))
+        return tgv_batch_run_fused(nvol, f, u, L, lams, alpha1, alpha0, iters, L2, epsil, infos, s);
     std::vector<TgvBatchVol> vols(nvol);
     long long ntiles = 0, nptiles = 0;
     size_t state_floats = 0;

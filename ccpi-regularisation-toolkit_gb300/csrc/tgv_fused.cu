@@ -40,17 +40,19 @@ __device__ __forceinline__ float bwd(float x, float xprev, bool first, bool last
     return first ? x : (last ? -xprev : x - xprev);
 }
 
-template <bool CHECK>
-__global__ void __launch_bounds__(NT, 2) k_tgv_fused(TgvFusedArgs a, Dims d, int zc, const StopCtl* ctl,
-                                                     double2* partials) {
+// One tile (bx, by, bz) of one volume; A is the argument block, a kernel
+// parameter or (batched runs) a volatile copy in shared memory, read at each
+// use rather than held in registers.
+template <bool CHECK, class A>
+__device__ __forceinline__ void fused_tile(A& a, const Dims& d, int zc, int bx, int by, int bz, float& pa_out,
+                                           float& pb_out) {
     __shared__ float sUV[4][BY * BX];  // U, V1..V3 of plane j
     __shared__ float sPQ[7][BY * BX];  // new P1, P2, Q1, Q2, Q4, Q5, Q6 of plane j
-    if (ctl->stop) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int x = blockIdx.x * OX + tx - 1;
-    const int y = blockIdx.y * OY + ty - 1;
-    const int z0 = blockIdx.z * zc;
+    const int x = bx * OX + tx - 1;
+    const int y = by * OY + ty - 1;
+    const int z0 = bz * zc;
     const int z1 = min(z0 + zc, nz);
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
     const bool d_pt = in_xy && tx <= BX - 2 && ty <= BY - 2;   // dual formed here
@@ -191,7 +193,38 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_fused(TgvFusedArgs a, Dims d, int
             nw[i] = fw[i];
         }
     }
+    pa_out = pa;
+    pb_out = pb;
+}
+
+template <bool CHECK>
+__global__ void __launch_bounds__(NT, 2) k_tgv_fused(TgvFusedArgs a, Dims d, int zc, const StopCtl* ctl,
+                                                     double2* partials) {
+    if (ctl->stop) return;
+    float pa = 0.f, pb = 0.f;
+    fused_tile<CHECK, const TgvFusedArgs>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+}
+
+// one iteration of every volume of a batch: a flat grid over all volumes'
+// tiles; `parity` selects the (old, new) buffer pair of the iteration
+template <bool CHECK>
+__global__ void __launch_bounds__(NT, 2) k_tgv_fused_batch(const TgvFusedVol* __restrict__ vols,
+                                                           const int* __restrict__ tile_vol, int parity) {
+    __shared__ TgvFusedArgs sa;
+    const long long t = blockIdx.x;
+    const TgvFusedVol& V = vols[tile_vol[t]];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    const int bx = (int)(lt % V.gx);
+    const int by = (int)((lt / V.gx) % V.gy);
+    const int bz = (int)(lt / ((long long)V.gx * V.gy));
+    if (threadIdx.x == 0 && threadIdx.y == 0) sa = V.args[parity];
+    __syncthreads();
+    const volatile TgvFusedArgs& va = sa;
+    float pa = 0.f, pb = 0.f;
+    fused_tile<CHECK, const volatile TgvFusedArgs>(va, V.d, V.zc, bx, by, bz, pa, pb);
+    if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
 }
 
 }  // namespace
@@ -208,6 +241,24 @@ TgvPlan tgv_fused_plan(const Dims& d) {
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
     return T;
+}
+
+void tgv_fused_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc) {
+    zc = (d.nz < ZCHUNK) ? d.nz : ZCHUNK;
+    gx = (d.nx + OX - 1) / OX;
+    gy = (d.ny + OY - 1) / OY;
+    gz = (d.nz + zc - 1) / zc;
+}
+
+int tgv_fused_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, long long ntiles, int parity, int check,
+                         cudaStream_t s) {
+    if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    if (check)
+        k_tgv_fused_batch<true><<<dim3((unsigned)ntiles), dim3(BX, BY, 1), 0, s>>>(d_vols, d_tile_vol, parity);
+    else
+        k_tgv_fused_batch<false><<<dim3((unsigned)ntiles), dim3(BX, BY, 1), 0, s>>>(d_vols, d_tile_vol, parity);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
 }
 
 int tgv_fused_step(const TgvPlan& T, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl, int check,

@@ -38,6 +38,20 @@ struct TgvFusedArgs {
     float lambda, alpha1, alpha0, tau, sigma, inv_lt;
 };
 TgvPlan tgv_fused_plan(const Dims& d);
+
+// one volume of a batched run of the fused pass (device descriptor table)
+struct TgvFusedVol {
+    Dims d;
+    TgvFusedArgs args[2];  // iteration parity 0: buffers 0 -> 1, parity 1: 1 -> 0
+    StopCtl* ctl;
+    double2* partials;     // one slot per tile of this volume
+    long long tile_base;   // first flat tile index of this volume
+    int gx, gy, gz, zc;
+};
+// tiling of the fused pass in a batched run (64-plane chunks)
+void tgv_fused_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);
+int tgv_fused_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, long long ntiles, int parity, int check,
+                         cudaStream_t s);
 int tgv_fused_step(const TgvPlan& T, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl, int check,
                    double2* partials, cudaStream_t s);
 
