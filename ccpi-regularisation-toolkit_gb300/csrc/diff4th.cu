@@ -128,6 +128,16 @@ int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters,
         // fused iteration, ping-pong between u_out and W's buffer
         float* bufs[2] = {u_out, W};
         int it = 0;
+        if (!ctl.checking() && d.n <= (1LL << 22)) {
+            // small volume, fixed count: launch overhead dominates, replay a graph
+            CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+                CILREG_TRY(d4_stream_step(T, bufs[k & 1], bufs[(k + 1) & 1], f, lam, tau, isg2, d, ctl.ctl(), 0,
+                                          ctl.partials(), st));
+                note_launch();
+                return OK;
+            }));
+            it = iters;
+        }
         for (; it < iters; it++) {
             const int check = ctl.is_check(it) ? 1 : 0;
             CILREG_TRY(d4_stream_step(T, bufs[it & 1], bufs[(it + 1) & 1], f, lam, tau, isg2, d, ctl.ctl(), check,

@@ -214,6 +214,18 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
     CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     const bool three = d.nz > 1;
     int it = 0;
+    if (!ctl.checking() && d.n <= (1LL << 22)) {
+        // small volume, fixed count: launch overhead dominates, replay a graph
+        auto kern = three ? k_llt_stream<true, false, int> : k_llt_stream<false, false, int>;
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+            kern<<<T.grid, T.block, 0, st>>>(bufs[k & 1], bufs[(k + 1) & 1], f, lam_rof, lam_llt, tau, d, T.zchunk,
+                                             ctl.ctl(), ctl.partials());
+            CILREG_CUDA(cudaGetLastError());
+            note_launch();
+            return OK;
+        }));
+        it = iters;
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         decltype(&k_llt_stream<true, true, int>) kern;

@@ -97,6 +97,24 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     float* bufs[2] = {u_out, alt};
     CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
+    if (!ctl.checking() && d.n <= (1LL << 22)) {
+        // small volume, fixed count: launch overhead dominates, replay a graph
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+            if (T.use)
+                CILREG_TRY(ndf_stream_step(T, pen, bufs[k & 1], bufs[(k + 1) & 1], f, lam, sg, isg, tau, d,
+                                           ctl.ctl(), 0, ctl.partials(), st));
+            else if (three)
+                launch_ndf<true>(pen, L, st, bufs[k & 1], bufs[(k + 1) & 1], f, lam, sg, isg, tau, d, ctl.ctl(), 0,
+                                 ctl.partials());
+            else
+                launch_ndf<false>(pen, L, st, bufs[k & 1], bufs[(k + 1) & 1], f, lam, sg, isg, tau, d, ctl.ctl(), 0,
+                                  ctl.partials());
+            CILREG_CUDA(cudaGetLastError());
+            note_launch();
+            return OK;
+        }));
+        it = iters;
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         if (T.use)

@@ -139,6 +139,32 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
     const float sigma = (float)(1.0 / (double)(lipschitz * tau));
     const float lt = tau / lam;
     int it = 0;
+    if (stream && !ctl.checking() && d.n <= (1LL << 22)) {
+        // small volume, fixed count: launch overhead dominates, replay a graph
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+            PdStreamArgs b;
+            b.u = ub[k & 1];
+            b.un = ub[(k + 1) & 1];
+            for (int c = 0; c < 3; c++) {
+                b.p[c] = pb[k & 1][c];
+                b.pn[c] = pb[(k + 1) & 1][c];
+            }
+            b.f = f;
+            b.ubrk = u_out;
+            b.sigma = sigma;
+            b.tau = tau;
+            b.lt = lt;
+            b.inv_onelt = (float)(1.0 / (1.0 + (double)lt));  // the reference divides by (1.0 + lt)
+            b.theta = 1.0f;
+            b.nonneg = (nonneg == 1);
+            b.aniso = (methodTV != 0);
+            b.check = 0;
+            CILREG_TRY(pd_stream_step(T, b, d, ctl.ctl(), ctl.partials(), st));
+            note_launch();
+            return OK;
+        }));
+        it = iters;
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         PdArgs a;

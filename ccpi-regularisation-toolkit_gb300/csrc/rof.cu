@@ -146,6 +146,14 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
     float* bufs[2] = {u_out, alt};
     CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
+    if (!ctl.checking() && d.n <= (1LL << 22)) {
+        // small volume, fixed count: launch overhead dominates, replay a graph
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+            return rof_launch_step(bufs[k & 1], bufs[(k + 1) & 1], f, lam_arr, lam, tau, d, ctl.ctl(), 0, nullptr,
+                                   st);
+        }));
+        it = iters;
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         const float* cur = bufs[it & 1];

@@ -122,6 +122,15 @@ inline dim3 grid1(long long n) {
     return dim3((unsigned)(b < 1 ? 1 : b));
 }
 
+// Fixed-count iteration loops on small volumes, where a launch costs about as
+// much as the kernel: enqueue(it, stream) for it in [0, iters), with
+// iterations [0, G) captured once into a CUDA graph and the graph replayed
+// while G or more remain, the rest launched directly, all on this thread's
+// own stream joined to `s` by events.  Only for loops whose launches depend
+// on `it` through its parity alone (G is even).
+template <class Enq>
+int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue);
+
 // process-wide count of kernels this library has launched (for benchmarks)
 void note_launch(long long n = 1);
 long long launch_count();
@@ -147,5 +156,65 @@ int launch_copy(float* dst, const float* src, long long n, cudaStream_t s);
 // buffer bufs[(last+1) & 1] holds it (ping-pong with iteration it writing bufs[(it+1)&1]).
 int launch_select_pingpong(const StopCtl* ctl, int iter_total, float* const bufs[2], float* dst, long long n,
                            cudaStream_t s);
+
+
+template <class Enq>
+int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue) {
+    const int reps = (G > 0 && (G % 2) == 0) ? iters / G : 0;
+    // a stream the caller is capturing records the launches as they are
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturing = cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+    cudaGetLastError();
+    if (reps < 2 || capturing) {
+        for (int it = 0; it < iters; it++) CILREG_TRY(enqueue(it, s));
+        return OK;
+    }
+    // capture and replay on this thread's own stream t (the caller's may be a
+    // default stream, which cannot be captured), ordered after the caller's
+    // earlier work and before its later work by two events
+    int dev = 0;
+    CILREG_CUDA(cudaGetDevice(&dev));
+    cudaStream_t t = thread_stream(dev);
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (int i = 0; i < 2; i++) CILREG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+    auto finish = [&](int rc) {
+        for (int i = 0; i < 2; i++) cudaEventDestroy(ev[i]);
+        return rc;
+    };
+    if (t != s) {
+        if (cudaEventRecord(ev[0], s) != cudaSuccess || cudaStreamWaitEvent(t, ev[0], 0) != cudaSuccess)
+            return finish(fail(ERR_CUDA, __FILE__, __LINE__, "stream ordering failed"));
+    }
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (cudaStreamBeginCapture(t, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return finish(fail(ERR_CUDA, __FILE__, __LINE__, "stream capture failed"));
+    const long long before = launch_count();
+    int rc = OK;
+    for (int k = 0; k < G && rc == OK; k++) rc = enqueue(k, t);
+    const cudaError_t e = cudaStreamEndCapture(t, &g);
+    if (rc != OK) {
+        if (g) cudaGraphDestroy(g);
+        return finish(rc);
+    }
+    if (e != cudaSuccess) return finish(fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(e)));
+    const cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return finish(fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(ei)));
+    const long long per_graph = launch_count() - before;
+    cudaError_t el = cudaSuccess;
+    for (int r = 0; r < reps && el == cudaSuccess; r++) el = cudaGraphLaunch(ge, t);
+    cudaGraphExecDestroy(ge);  // freed when the queued launches complete
+    if (el != cudaSuccess) return finish(fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(el)));
+    note_launch(per_graph * (reps - 1));  // the capture counted one replay
+    for (int it = reps * G; it < iters && rc == OK; it++) rc = enqueue(it, t);
+    if (rc != OK) return finish(rc);
+    if (t != s) {
+        if (cudaEventRecord(ev[1], t) != cudaSuccess || cudaStreamWaitEvent(s, ev[1], 0) != cudaSuccess)
+            return finish(fail(ERR_CUDA, __FILE__, __LINE__, "stream ordering failed"));
+    }
+    return finish(OK);
+}
+
 
 }  // namespace cilreg
