@@ -130,7 +130,7 @@ int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters,
         int it = 0;
         if (!ctl.checking() && d.n <= (1LL << 22)) {
             // small volume, fixed count: launch overhead dominates, replay a graph
-            CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+            CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
                 CILREG_TRY(d4_stream_step(T, bufs[k & 1], bufs[(k + 1) & 1], f, lam, tau, isg2, d, ctl.ctl(), 0,
                                           ctl.partials(), st));
                 note_launch();

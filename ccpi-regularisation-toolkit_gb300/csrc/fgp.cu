@@ -165,6 +165,38 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     };
     auto writes_p = [&](int k) { return (k != iters - 1) || warm != nullptr; };
     int it = 0;
+    constexpr int G = 66;  // replayed block: a multiple of the ring's period 3, even
+    if (T.use && !tma && !TP.use && !ctl.checking() && d.n <= (1LL << 22) && iters > 2 * G) {
+        // small volume, fixed count: iterations 0 .. iters-2 from a replayed
+        // graph, their momentum coefficients read on the device from the
+        // sequence formed here (FGP_TV_core.c:138-139); the last one directly
+        std::vector<float> cseq(iters);
+        for (int k = 0; k < iters; k++) {
+            cseq[k] = cprev;
+            const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;
+            cprev = (tk - 1.0f) / tkp1;
+            tk = tkp1;
+        }
+        float* carr = scratch.floats(iters);
+        int* cbase = (int*)scratch.bytes(sizeof(int));
+        if (!carr || !cbase) return scratch.status();
+        CILREG_CUDA(cudaMemcpyAsync(carr, cseq.data(), sizeof(float) * iters, cudaMemcpyHostToDevice, s));
+        CILREG_CUDA(cudaMemsetAsync(cbase, 0, sizeof(int), s));
+        auto iteration = [&](int k, cudaStream_t st, bool in_graph) -> int {
+            float* pn[3] = {ring[k % R][0], ring[k % R][1], ring[k % R][2]};
+            const float* pc[3] = {ring[(k + R - 1) % R][0], ring[(k + R - 1) % R][1], ring[(k + R - 1) % R][2]};
+            const float* po[3] = {ring[(k + R - 2) % R][0], ring[(k + R - 2) % R][1], ring[(k + R - 2) % R][2]};
+            CILREG_TRY(fgp_tiled_step(T, pc, po, pn, f, u_out, lam, cseq[k], multip, nonneg == 1, methodTV != 0,
+                                      writes_u(k) ? 1 : 0, writes_p(k) ? 1 : 0, 0, d, ctl.ctl(), nullptr, st, nullptr,
+                                      in_graph ? carr : nullptr, cbase, k));
+            note_launch();
+            return OK;
+        };
+        CILREG_TRY(run_replayed(iters - 1, G, s, iteration,
+                                [&](cudaStream_t st) -> int { return fgp_advance_base(cbase, G, st); }));
+        CILREG_TRY(iteration(iters - 1, s, false));
+        it = iters;
+    }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         if (TP.use && it + 1 < iters && !check && !ctl.is_check(it + 1) && !writes_u(it) && writes_p(it)) {

@@ -40,6 +40,10 @@ struct TiledArgs {
     float lam, c, multip;
     int nonneg, aniso, write_u, write_p, check;
     const float* b[3];  // FGP-dTV only: unit gradient field of the reference image
+    // momentum from device memory (graph replays): c = carr[*cbase + coff]
+    const float* carr;
+    const int* cbase;
+    int coff;
 };
 
 // One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk.
@@ -96,12 +100,13 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
     float b1p = 0.f, b2p = 0.f, b3p = 0.f;            // dTV: unit gradient of plane k-1
     float uo = 0.f;  // U_prev of the plane the next P step writes (stopping checks only)
     float pa = 0.f, pb = 0.f;
+    const float cm = a.carr ? a.carr[*a.cbase + a.coff] : a.c;
     load_plane(z0 - 1);
     for (int k = z0 - 1; k <= z1; ++k) {
         // 1. R of plane k from the prefetched values; start loading plane k+1
-        float r1 = c1 + a.c * (c1 - o1);
-        float r2 = c2 + a.c * (c2 - o2);
-        float r3 = THREE ? (c3 + a.c * (c3 - o3)) : 0.f;
+        float r1 = c1 + cm * (c1 - o1);
+        float r2 = c2 + cm * (c2 - o2);
+        float r3 = THREE ? (c3 + cm * (c3 - o3)) : 0.f;
         const float fk = fv;
         const float b1 = e1, b2 = e2, b3 = e3;
         if (DTV) {
@@ -226,6 +231,9 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* _
     a.write_p = write_p;
     a.check = CHECK;
     a.b[0] = a.b[1] = a.b[2] = nullptr;
+    a.carr = nullptr;
+    a.cbase = nullptr;
+    a.coff = 0;
     float pa = 0.f, pb = 0.f;
     fgp_stream_tile<THREE, CHECK, IT>(a, V.d, V.zc, bx, by, bz, pa, pb);
     if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
@@ -259,6 +267,15 @@ int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long n
 
 int fgp_default_zchunk(const Dims& d) { return (d.nz > 1) ? ((d.nz < ZCHUNK) ? d.nz : ZCHUNK) : 1; }
 
+__global__ void k_add_int(int* p, int v) { *p += v; }
+
+int fgp_advance_base(int* base, int by, cudaStream_t s) {
+    k_add_int<<<1, 1, 0, s>>>(base, by);
+    CILREG_CUDA(cudaGetLastError());
+    note_launch();
+    return OK;
+}
+
 TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm) {
     TiledPlan T;
     const char* e = getenv("CILREG_FGP_KERNEL");
@@ -281,8 +298,11 @@ TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm) {
 int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
-                   const float* const* b) {
+                   const float* const* b, const float* carr, const int* cbase, int coff) {
     TiledArgs a;
+    a.carr = carr;
+    a.cbase = cbase;
+    a.coff = coff;
     for (int i = 0; i < 3; i++) {
         a.pc[i] = pc[i];
         a.po[i] = po[i];

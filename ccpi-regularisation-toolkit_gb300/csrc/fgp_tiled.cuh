@@ -17,11 +17,16 @@ TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm = 0);
 int fgp_default_zchunk(const Dims& d);
 
 // one FGP iteration; with `b` (three device arrays, the unit gradient field
-// of a reference image) one FGP-dTV iteration instead
+// of a reference image) one FGP-dTV iteration instead; with `carr` the
+// momentum coefficient is read on the device as carr[*cbase + coff] (c is
+// then unused), so a captured iteration can be replayed at other indices
 int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
-                   const float* const* b = nullptr);
+                   const float* const* b = nullptr, const float* carr = nullptr, const int* cbase = nullptr,
+                   int coff = 0);
+// *base += by on the device (one thread)
+int fgp_advance_base(int* base, int by, cudaStream_t s);
 
 // Two iterations k, k+1 in one streaming pass (fgp_pair.cu; 3D only).
 struct PairPlan {

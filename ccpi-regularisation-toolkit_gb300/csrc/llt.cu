@@ -217,7 +217,7 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
         auto kern = three ? k_llt_stream<true, false, int> : k_llt_stream<false, false, int>;
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             kern<<<T.grid, T.block, 0, st>>>(bufs[k & 1], bufs[(k + 1) & 1], f, lam_rof, lam_llt, tau, d, T.zchunk,
                                              ctl.ctl(), ctl.partials());
             CILREG_CUDA(cudaGetLastError());

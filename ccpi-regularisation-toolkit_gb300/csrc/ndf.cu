@@ -99,7 +99,7 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     int it = 0;
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             if (T.use)
                 CILREG_TRY(ndf_stream_step(T, pen, bufs[k & 1], bufs[(k + 1) & 1], f, lam, sg, isg, tau, d,
                                            ctl.ctl(), 0, ctl.partials(), st));

@@ -141,7 +141,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
     int it = 0;
     if (stream && !ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             PdStreamArgs b;
             b.u = ub[k & 1];
             b.un = ub[(k + 1) & 1];

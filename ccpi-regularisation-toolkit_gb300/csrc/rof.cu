@@ -148,7 +148,7 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
     int it = 0;
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             return rof_launch_step(bufs[k & 1], bufs[(k + 1) & 1], f, lam_arr, lam, tau, d, ctl.ctl(), 0, nullptr,
                                    st);
         }));

@@ -3,6 +3,8 @@
 // control.  Nothing here synchronises the device per iteration.
 #pragma once
 
+#include <stdlib.h>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -123,13 +125,17 @@ inline dim3 grid1(long long n) {
 }
 
 // Fixed-count iteration loops on small volumes, where a launch costs about as
-// much as the kernel: enqueue(it, stream) for it in [0, iters), with
-// iterations [0, G) captured once into a CUDA graph and the graph replayed
-// while G or more remain, the rest launched directly, all on this thread's
-// own stream joined to `s` by events.  Only for loops whose launches depend
-// on `it` through its parity alone (G is even).
-template <class Enq>
-int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue);
+// much as the kernel: enqueue(it, stream, in_graph) for it in [0, iters),
+// with iterations [0, G) captured once into a CUDA graph (in_graph true; then
+// tail(stream), which may advance device-side iteration state) and the graph
+// replayed while G or more remain, the rest launched directly, all on this
+// thread's own stream joined to `s` by events.  Only for loops whose launches
+// depend on `it` through `it mod G` (G even) or on device-side state.
+struct NoTail {
+    int operator()(cudaStream_t) const { return 0; }
+};
+template <class Enq, class Tail = NoTail>
+int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue, Tail tail = Tail());
 
 // process-wide count of kernels this library has launched (for benchmarks)
 void note_launch(long long n = 1);
@@ -158,15 +164,16 @@ int launch_select_pingpong(const StopCtl* ctl, int iter_total, float* const bufs
                            cudaStream_t s);
 
 
-template <class Enq>
-int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue) {
-    const int reps = (G > 0 && (G % 2) == 0) ? iters / G : 0;
+template <class Enq, class Tail>
+int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue, Tail tail) {
+    const char* env = getenv("CILREG_GRAPH_REPLAY");  // "0": launch every iteration directly (A/B checks)
+    const int reps = (G > 0 && (G % 2) == 0 && !(env && env[0] == '0')) ? iters / G : 0;
     // a stream the caller is capturing records the launches as they are
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     const bool capturing = cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
     cudaGetLastError();
     if (reps < 2 || capturing) {
-        for (int it = 0; it < iters; it++) CILREG_TRY(enqueue(it, s));
+        for (int it = 0; it < iters; it++) CILREG_TRY(enqueue(it, s, false));
         return OK;
     }
     // capture and replay on this thread's own stream t (the caller's may be a
@@ -191,7 +198,8 @@ int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue) {
         return finish(fail(ERR_CUDA, __FILE__, __LINE__, "stream capture failed"));
     const long long before = launch_count();
     int rc = OK;
-    for (int k = 0; k < G && rc == OK; k++) rc = enqueue(k, t);
+    for (int k = 0; k < G && rc == OK; k++) rc = enqueue(k, t, true);
+    if (rc == OK) rc = tail(t);
     const cudaError_t e = cudaStreamEndCapture(t, &g);
     if (rc != OK) {
         if (g) cudaGraphDestroy(g);
@@ -207,7 +215,7 @@ int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue) {
     cudaGraphExecDestroy(ge);  // freed when the queued launches complete
     if (el != cudaSuccess) return finish(fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(el)));
     note_launch(per_graph * (reps - 1));  // the capture counted one replay
-    for (int it = reps * G; it < iters && rc == OK; it++) rc = enqueue(it, t);
+    for (int it = reps * G; it < iters && rc == OK; it++) rc = enqueue(it, t, false);
     if (rc != OK) return finish(rc);
     if (t != s) {
         if (cudaEventRecord(ev[1], t) != cudaSuccess || cudaStreamWaitEvent(s, ev[1], 0) != cudaSuccess)

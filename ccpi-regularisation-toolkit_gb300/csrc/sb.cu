@@ -206,7 +206,7 @@ int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int m
             w.u2 = bufs[1];
             CILREG_TRY(sb_sweep2_step(T, w, d, ctl.ctl(), 0, ctl.partials(), s));
             note_launch();
-            CILREG_TRY(run_replayed(iters - 1, 64, s, [&](int k, cudaStream_t st) -> int {
+            CILREG_TRY(run_replayed(iters - 1, 64, s, [&](int k, cudaStream_t st, bool) -> int {
                 const int i = k + 1;
                 z.u = bufs[i & 1];
                 z.u2 = bufs[(i + 1) & 1];

@@ -369,7 +369,7 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
     int it = 0;
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             set_parity(k);
             CILREG_TRY(tgv_fused_step(T, a, d, ctl.ctl(), 0, ctl.partials(), st));
             note_launch();
@@ -445,7 +445,7 @@ int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0,
     if (T.use && !ctl.checking() && d.n <= (1LL << 22)) {
         // small volume (2D here), fixed count: launch overhead dominates, replay a graph
         a.check = 0;
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int, cudaStream_t st) -> int {
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int, cudaStream_t st, bool) -> int {
             CILREG_TRY(tgv_dual_stream_step(T, a, d, ctl.ctl(), st));
             CILREG_TRY(tgv_primal_stream_step(T, a, d, ctl.ctl(), ctl.partials(), st));
             note_launch(2);
