@@ -8,6 +8,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 namespace cilreg {
 
@@ -194,6 +195,39 @@ __global__ void __launch_bounds__(1024) k_finalize_check(const double2* __restri
     }
 }
 
+namespace {
+
+// pinned mirrors of the stop control, kept per host thread and reused across
+// calls (cudaMallocHost / cudaFreeHost per call cost tens of microseconds and
+// the free can wait for the device); a small stack, since calls may nest
+struct PinnedMirrors {
+    std::vector<StopCtl*> free_list;
+    ~PinnedMirrors() {
+        // process exit: the CUDA context may already be gone, so leave them
+    }
+};
+thread_local PinnedMirrors t_mirrors;
+
+StopCtl* take_mirror() {
+    if (!t_mirrors.free_list.empty()) {
+        StopCtl* p = t_mirrors.free_list.back();
+        t_mirrors.free_list.pop_back();
+        return p;
+    }
+    StopCtl* p = nullptr;
+    if (cudaMallocHost((void**)&p, sizeof(StopCtl) * 5) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void give_mirror(StopCtl* p) {
+    if (p) t_mirrors.free_list.push_back(p);
+}
+
+}  // namespace
+
 IterControl::IterControl(cudaStream_t s, Scratch& scratch, int iter_total, float epsil, long long max_partials)
     : stream_(s), epsil_(epsil) {
     d_ctl_ = (StopCtl*)scratch.bytes(sizeof(StopCtl));
@@ -206,9 +240,8 @@ IterControl::IterControl(cudaStream_t s, Scratch& scratch, int iter_total, float
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { status_ = fail(ERR_CUDA, __FILE__, __LINE__, "%s", cudaGetErrorString(e)); return; }
-    if (cudaMallocHost((void**)&h_ring_, sizeof(StopCtl) * 5) != cudaSuccess) {
+    if (!(h_ring_ = take_mirror())) {
         status_ = fail(ERR_CUDA, __FILE__, __LINE__, "pinned allocation failed");
-        h_ring_ = nullptr;
         return;
     }
     memset(h_ring_, 0, sizeof(StopCtl) * 5);
@@ -228,7 +261,7 @@ IterControl::~IterControl() {
     // the pinned mirror that pending copies may still target
     if (h_ring_) {
         cudaStreamSynchronize(stream_);
-        cudaFreeHost(h_ring_);
+        give_mirror(h_ring_);
     }
     for (int i = 0; i < nev_; i++) cudaEventDestroy(ev_[i]);
 }
@@ -276,7 +309,7 @@ int IterControl::finish(float* infovector, StopCtl* out) {
     if (out) *out = c;
     for (int i = 0; i < nev_; i++) cudaEventDestroy(ev_[i]);
     nev_ = 0;
-    cudaFreeHost(h_ring_);
+    give_mirror(h_ring_);
     h_ring_ = nullptr;
     return OK;
 }
