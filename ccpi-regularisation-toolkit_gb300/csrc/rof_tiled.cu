@@ -29,10 +29,15 @@
 #include <type_traits>
 
 #include "rof_tiled.cuh"
+#include "tma_ring.cuh"
 
 namespace cilreg {
 
 namespace {
+
+using tma::cp_async4;
+using tma::cp_async_commit;
+using tma::cp_async_wait;
 
 constexpr int BX = 32, BY = 16;
 constexpr int OX = BX - 2, OY = BY - 2;  // updated voxels per tile
@@ -195,17 +200,6 @@ __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ 
         if (j <= z1 + 1) step(Ic<0>{}, std::true_type{}, j);
     }
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
-}
-
-// cp.async (sm_80+ asynchronous global -> shared copies, 4 bytes per thread)
-__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // The 3D iteration with U staged through shared memory by asynchronous copies

@@ -9,6 +9,8 @@
 // unless CILREG_TGV_KERNEL=simple.
 // 3D state: U, P(3), Q(6), V(3) plus U0.  The dual and primal halves of the
 // reference's ten sweeps (TGV_core.c:136-167) collapse into these two.
+#include <vector>
+
 #include "drivers.cuh"
 #include "tgv_batch.cuh"
 #include "tgv_tiled.cuh"
@@ -351,6 +353,11 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
     a.tau = (float)pow((double)L2, -0.5);  // TGV_core.c:54-55
     a.sigma = a.tau;
     a.inv_lt = 1.0f / (a.lambda + a.tau);
+    // tensor maps of the staged pass, one set per buffer parity (the pass that
+    // loads by threads runs on the same tiling if an array is misaligned)
+    const size_t mb = tgv_tma_maps_bytes();
+    std::vector<unsigned char> maps(T.tma ? 2 * mb : 0);
+    bool tma = T.tma;
     auto set_parity = [&](int k) {
         const int cur = k & 1, nxt = cur ^ 1;
         a.u = ub[cur];
@@ -366,12 +373,20 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
             a.qn[c] = qb[nxt][c];
         }
     };
+    for (int k = 0; k < 2 && tma; k++) {
+        set_parity(k);
+        tma = tgv_tma_encode(a, d, maps.data() + mb * k);
+    }
+    auto step = [&](int k, int check, cudaStream_t st) -> int {
+        if (tma) return tgv_tma_step(T, maps.data() + mb * (k & 1), a, d, ctl.ctl(), check, ctl.partials(), st);
+        return tgv_fused_step(T, a, d, ctl.ctl(), check, ctl.partials(), st);
+    };
     int it = 0;
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
         CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
             set_parity(k);
-            CILREG_TRY(tgv_fused_step(T, a, d, ctl.ctl(), 0, ctl.partials(), st));
+            CILREG_TRY(step(k, 0, st));
             note_launch();
             return OK;
         }));
@@ -379,20 +394,8 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
     }
     for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
-        const int cur = it & 1, nxt = cur ^ 1;
-        a.u = ub[cur];
-        a.un = ub[nxt];
-        for (int c = 0; c < 3; c++) {
-            a.v[c] = vb[cur][c];
-            a.vn[c] = vb[nxt][c];
-            a.p[c] = pb[cur][c];
-            a.pn[c] = pb[nxt][c];
-        }
-        for (int c = 0; c < 6; c++) {
-            a.q[c] = qb[cur][c];
-            a.qn[c] = qb[nxt][c];
-        }
-        CILREG_TRY(tgv_fused_step(T, a, d, ctl.ctl(), check, ctl.partials(), s));
+        set_parity(it);
+        CILREG_TRY(step(it, check, s));
         note_launch();
         if (check) {
             CILREG_TRY(ctl.after_check(it, T.nblocks));
@@ -400,6 +403,7 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
         }
     }
     if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl.ctl(), iters, ub, u_out, d.n, s));
+    if (tma) CILREG_TRY(tgv_tma_status(s));
     return ctl.finish(info);
 }
 

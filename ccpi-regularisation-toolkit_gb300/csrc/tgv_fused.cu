@@ -22,6 +22,7 @@
 // passes' iterates bit for bit.
 #include <type_traits>
 
+#include "tgv_fused_math.cuh"
 #include "tgv_tiled.cuh"
 
 namespace cilreg {
@@ -35,10 +36,6 @@ constexpr int ZCHUNK = 64;
 
 template <int V>
 using Ic = std::integral_constant<int, V>;
-
-__device__ __forceinline__ float bwd(float x, float xprev, bool first, bool last) {
-    return first ? x : (last ? -xprev : x - xprev);
-}
 
 // One tile (bx, by, bz) of one volume; A is the argument block, a kernel
 // parameter or (batched runs) a volatile copy in shared memory, read at each
@@ -93,101 +90,52 @@ __device__ __forceinline__ void fused_tile(A& a, const Dims& d, int zc, int bx, 
         for (int i = 0; i < 4; i++) sUV[i][oc] = cw[i];
         __syncthreads();
         // 2. dual half at plane j (DualP_3D + ProjP_3D, DualQ_3D + ProjQ_3D)
-        float p1 = 0.f, p2 = 0.f, p3 = 0.f, Q1 = 0.f, Q2 = 0.f, Q3 = 0.f, Q4 = 0.f, Q5 = 0.f, Q6 = 0.f;
+        TgvDual n{};
         if (d_pt && plane_ok) {
-            const bool ze = (j == nz - 1);
-            const float u = cw[0], v1 = cw[1], v2 = cw[2], v3 = cw[3];
-            p1 = pq[0] + (xe ? sigma * (-v1) : sigma * ((sUV[0][oxh] - u) - v1));
-            p2 = pq[1] + (ye ? sigma * (-v2) : sigma * ((sUV[0][oyh] - u) - v2));
-            p3 = pq[2] + (ze ? sigma * (-v3) : sigma * ((nw[0] - u) - v3));
-            const float gp = sqrtf(p1 * p1 + p2 * p2 + p3 * p3) / alpha1;
-            if (gp > 1.0f) {
-                const float ig = __frcp_rn(gp);
-                p1 *= ig;
-                p2 *= ig;
-                p3 *= ig;
-            }
-            float q1 = 0.f, q11 = 0.f, q33 = 0.f, q2 = 0.f, q22 = 0.f, q55 = 0.f, q3 = 0.f, q44 = 0.f, q66 = 0.f;
-            if (!xe) {
-                q1 = sUV[1][oxh] - v1;
-                q11 = sUV[2][oxh] - v2;
-                q33 = sUV[3][oxh] - v3;
-            }
-            if (!ye) {
-                q2 = sUV[2][oyh] - v2;
-                q22 = sUV[1][oyh] - v1;
-                q55 = sUV[3][oyh] - v3;
-            }
-            if (!ze) {
-                q3 = nw[3] - v3;
-                q44 = nw[1] - v1;
-                q66 = nw[2] - v2;
-            }
-            Q1 = pq[3] + sigma * q1;
-            Q2 = pq[4] + sigma * q2;
-            Q3 = pq[5] + sigma * q3;
-            Q4 = pq[6] + sigma * (0.5f * (q11 + q22));
-            Q5 = pq[7] + sigma * (0.5f * (q33 + q44));
-            Q6 = pq[8] + sigma * (0.5f * (q55 + q66));
-            float g = sqrtf(Q1 * Q1 + Q2 * Q2 + Q3 * Q3 + 2.0f * Q4 * Q4 + 2.0f * Q5 * Q5 + 2.0f * Q6 * Q6);
-            g = g / alpha0;
-            if (g > 1.0f) {
-                const float ig = __frcp_rn(g);
-                Q1 *= ig;
-                Q2 *= ig;
-                Q3 *= ig;
-                Q4 *= ig;
-                Q5 *= ig;
-                Q6 *= ig;
-            }
+            n = tgv_dual_voxel(
+                cw[0], cw[1], cw[2], cw[3], [&](int c) { return sUV[c][oxh]; }, [&](int c) { return sUV[c][oyh]; },
+                [&](int c) { return nw[c]; }, pq, xe, ye, j == nz - 1, sigma, alpha1, alpha0);
             if (o_pt && j >= z0) {
-                a.pn[0][o] = p1;
-                a.pn[1][o] = p2;
-                a.pn[2][o] = p3;
-                a.qn[0][o] = Q1;
-                a.qn[1][o] = Q2;
-                a.qn[2][o] = Q3;
-                a.qn[3][o] = Q4;
-                a.qn[4][o] = Q5;
-                a.qn[5][o] = Q6;
+                a.pn[0][o] = n.p1;
+                a.pn[1][o] = n.p2;
+                a.pn[2][o] = n.p3;
+                a.qn[0][o] = n.q1;
+                a.qn[1][o] = n.q2;
+                a.qn[2][o] = n.q3;
+                a.qn[3][o] = n.q4;
+                a.qn[4][o] = n.q5;
+                a.qn[5][o] = n.q6;
             }
         }
-        sPQ[0][oc] = p1;
-        sPQ[1][oc] = p2;
-        sPQ[2][oc] = Q1;
-        sPQ[3][oc] = Q2;
-        sPQ[4][oc] = Q4;
-        sPQ[5][oc] = Q5;
-        sPQ[6][oc] = Q6;
+        sPQ[0][oc] = n.p1;
+        sPQ[1][oc] = n.p2;
+        sPQ[2][oc] = n.q1;
+        sPQ[3][oc] = n.q2;
+        sPQ[4][oc] = n.q4;
+        sPQ[5][oc] = n.q5;
+        sPQ[6][oc] = n.q6;
         __syncthreads();
         // 3. primal half at plane j (DivProjP_3D + newU3D, UpdV_3D + newV)
         if (o_pt && j >= z0) {
             const bool zf = (j == 0), zl = (j == nz - 1);
-            const float cu = cw[0];
-            float dv = bwd(p1, sPQ[0][oxl], xf, xe) + bwd(p2, sPQ[1][oyl], yf, ye);
-            dv = dv + bwd(p3, zp3, zf, zl);
-            const float un = (lam * (cu + tau * dv) + tau * u0) * ilt;
-            const float ue = 2.0f * un - cu;
+            const float ue = tgv_primal_u(n, sPQ[0][oxl], sPQ[1][oyl], zp3, xf, xe, yf, ye, zf, zl, cw[0], u0, lam,
+                                          tau, ilt);
             a.un[o] = ue;
             if (CHECK) {
-                const float df = ue - cu;
+                const float df = ue - cw[0];
                 pa += df * df;
                 pb += ue * ue;
             }
-            const float q1 = bwd(Q1, sPQ[2][oxl], xf, xe), q4x = bwd(Q4, sPQ[4][oxl], xf, xe),
-                        q5x = bwd(Q5, sPQ[5][oxl], xf, xe);
-            const float q2 = bwd(Q2, sPQ[3][oyl], yf, ye), q4y = bwd(Q4, sPQ[4][oyl], yf, ye),
-                        q6y = bwd(Q6, sPQ[6][oyl], yf, ye);
-            const float q6z = bwd(Q6, zq6, zf, zl), q5z = bwd(Q5, zq5, zf, zl), q3 = bwd(Q3, zq3, zf, zl);
-            const float d1 = q1 + q4y + q5z, d2 = q4x + q2 + q6z, d3 = q5x + q6y + q3;
-            a.vn[0][o] = 2.0f * (cw[1] + tau * (p1 + d1)) - cw[1];
-            a.vn[1][o] = 2.0f * (cw[2] + tau * (p2 + d2)) - cw[2];
-            a.vn[2][o] = 2.0f * (cw[3] + tau * (p3 + d3)) - cw[3];
+            const TgvNewV w = tgv_primal_v(n, sPQ[2][oxl], sPQ[4][oxl], sPQ[5][oxl], sPQ[3][oyl], sPQ[4][oyl],
+                                           sPQ[6][oyl], zq3, zq5, zq6, xf, xe, yf, ye, zf, zl, cw[1], cw[2], cw[3], tau);
+            a.vn[0][o] = w.v1;
+            a.vn[1][o] = w.v2;
+            a.vn[2][o] = w.v3;
         }
-        zp3 = p3;
-        zq3 = Q3;
-        zq5 = Q5;
-        zq6 = Q6;
+        zp3 = n.p3;
+        zq3 = n.q3;
+        zq5 = n.q5;
+        zq6 = n.q6;
         for (int i = 0; i < 4; i++) {
             cw[i] = nw[i];
             nw[i] = fw[i];
@@ -235,9 +183,10 @@ TgvPlan tgv_fused_plan(const Dims& d) {
     T.use = d.nz > 1 && d.n < (1LL << 31) && !(e && e[0] == '0');
     if (!T.use) return T;
     static const int resident = resident_ctas(k_tgv_fused<false>, NT);
+    T.tma = tgv_tma_usable(d);
     T.block = dim3(BX, BY, 1);
     const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
-    T.zchunk = wave_zchunk(tiles, d.nz, resident, 1, ZCHUNK);
+    T.zchunk = wave_zchunk(tiles, d.nz, T.tma ? tgv_tma_resident() : resident, 1, ZCHUNK);
     T.grid = dim3((d.nx + OX - 1) / OX, (d.ny + OY - 1) / OY, (d.nz + T.zchunk - 1) / T.zchunk);
     T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
     return T;

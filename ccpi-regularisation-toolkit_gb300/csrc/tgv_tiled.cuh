@@ -10,6 +10,7 @@ struct TgvPlan {
     long long nblocks = 0;
     int zchunk = 0;
     bool use = false;  // false: the per-voxel kernels of tgv.cu run instead
+    bool tma = false;  // fused pass: inputs staged by tensor copies (tgv_fused_tma.cu)
 };
 
 TgvPlan tgv_primal_plan(const Dims& d);
@@ -54,6 +55,20 @@ int tgv_fused_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, long 
                          cudaStream_t s);
 int tgv_fused_step(const TgvPlan& T, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl, int check,
                    double2* partials, cudaStream_t s);
+
+// the fused pass with its 14 input arrays staged by tensor copies
+// (tgv_fused_tma.cu): 3D volumes whose x extent is a multiple of 4 and whose
+// arrays start on 16-byte boundaries; CILREG_TGV_TMA=0 turns it off
+bool tgv_tma_usable(const Dims& d);
+int tgv_tma_resident();  // CTAs per SM of the staged kernel (0 if it cannot run)
+size_t tgv_tma_maps_bytes();
+// tensor maps of a's input arrays into maps_out (tgv_tma_maps_bytes() bytes);
+// false if an array is not 16-byte aligned or the driver refuses a map
+bool tgv_tma_encode(const TgvFusedArgs& a, const Dims& d, void* maps_out);
+int tgv_tma_step(const TgvPlan& T, const void* maps, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl,
+                 int check, double2* partials, cudaStream_t s);
+// fails if a tensor-copy wait of the staged kernel ran out (and clears the flag)
+int tgv_tma_status(cudaStream_t s);
 
 // tiling of the streaming primal kernel in a batched run (64-plane chunks)
 void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);

@@ -1,5 +1,6 @@
 // Staging of input planes by the Tensor Memory Accelerator for the 2.5D
-// streaming kernels (used by fgp_tma.cu and pd_tma.cu).
+// streaming kernels (used by fgp_tma.cu and tgv_fused_tma.cu), and the
+// per-thread asynchronous copies (used by rof_tiled.cu and tgv_fused_tma.cu).
 //
 // A kernel keeps a ring of STAGES shared-memory stages, each holding the
 // tile's box of every input array for one plane, and one mbarrier per stage.
@@ -62,6 +63,17 @@ __device__ __forceinline__ bool wait_stage(uint64_t* bar, int use) {
     for (long long t = 0; t < WAIT_LIMIT; t++)
         if (mbar_try(bar, parity)) return true;
     return false;
+}
+
+// per-thread asynchronous global -> shared copies of 4 bytes (cp.async,
+// sm_80+), grouped per plane; a thread waits for its own groups only
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // host: cuTensorMapEncodeTiled from the driver (null if unavailable)

@@ -285,6 +285,27 @@ def test_fgp_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("shape", [(2, 30, 32), (3, 29, 16), (10, 16, 24), (67, 70, 12), (130, 33, 36), (65, 57, 28),
+                                   (200, 41, 60), (33, 100, 4), (70, 150, 256)], ids=str)
+def test_tgv_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
+    """The one-pass TGV iteration whose 14 input arrays are staged by tensor
+    copies (x extent a multiple of 4) gives the iterates of the thread-loading
+    pass bit for bit, and the same stopping iteration (graph-replayed runs of
+    small volumes and runs with the stopping rule alike)."""
+    from ccpi.filters.regularisers import TGV
+
+    rng = np.random.default_rng(29 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil, iters in ((0.0, 37), (3e-3, 80), (0.0, 1), (1e-4, 23)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = TGV(x, 0.05, 1.0, 2.0, iters, 12.0, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_TGV_TMA", "0")
+        b = TGV(x, 0.05, 1.0, 2.0, iters, 12.0, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_TGV_TMA")
+        assert int(ia[0]) == int(ib[0])
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("shape", [(2, 30, 31), (3, 29, 15), (10, 16, 22), (67, 70, 9), (130, 33, 35), (65, 57, 29),
                                    (200, 41, 60)], ids=str)
 def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
