@@ -58,6 +58,13 @@ __device__ __forceinline__ float normalise(float dp, float s) { return dp * rsqr
 template <int V>
 using Ic = std::integral_constant<int, V>;
 
+// the value of an integral constant or of a plain int, on the device
+template <int V>
+__device__ __forceinline__ constexpr int ival(Ic<V>) {
+    return V;
+}
+__device__ __forceinline__ int ival(int v) { return v; }
+
 // IT: element-offset type (int when the volume has fewer than 2^31 voxels)
 template <bool THREE, bool CHECK, bool LARR, typename IT>
 __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ U, float* __restrict__ Un,
@@ -242,7 +249,8 @@ __global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U
     const int z1 = min(z0 + zc, nz);
     const IT sxy = (IT)d.sxy;
     auto at = [&](int k) -> IT { return (IT)min(max(k, 0), nz - 1) * sxy + col; };
-    auto slot = [&](int k) -> float* { return sU[(k - z0 + 2) & (RING - 1)]; };
+    // ring slot of plane z0 + r - 2 (plane k sits in slot (k - z0 + 2) & 7)
+    auto slot_of = [&](int r) -> float* { return sU[r & (RING - 1)]; };
     auto ld_f = [&](int k, float& fv, float& lv) {
         const IT o = at(k);
         fv = o_pt ? __ldg(F + o) : 0.f;
@@ -251,24 +259,28 @@ __global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U
     float pa = 0.f, pb = 0.f;
     // planes z0-2 .. z0+AHEAD-1 in flight, one copy group per plane
     for (int k = z0 - 2; k < z0 + AHEAD; k++) {
-        cp_async4(slot(k) + oc, U + at(k));
+        cp_async4(slot_of(k - z0 + 2) + oc, U + at(k));
         cp_async_commit();
     }
     float fa = 0.f, la = lam, fb = 0.f, lb = lam;
     float d1o = 0.f, d2o = 0.f, d3o = 0.f, d3oo = 0.f;
 
-    auto step = [&](auto par, auto full, int j) {
-        constexpr int P = decltype(par)::value;       // flux ring slot of plane j
+    // step j, r = j - z0: an integral constant in the unrolled loop (every
+    // ring slot and the flux parity fold to constants), a plain int in the
+    // remainder
+    auto step = [&](auto rr, auto full, int j) {
+        const int r = ival(rr);
+        const int P = r & 1;                          // flux ring slot of plane j
         constexpr bool FULL = decltype(full)::value;  // plane j-2 is updated
-        cp_async4(slot(j + AHEAD) + oc, U + at(j + AHEAD));
+        cp_async4(slot_of(r + 2 + AHEAD) + oc, U + at(j + AHEAD));
         cp_async_commit();
         float fe, le;
         ld_f(j, fe, le);
         cp_async_wait<AHEAD>();  // this thread's copy of plane j has landed
         __syncthreads();         // ... and every thread's, and the fluxes of plane j-2
-        const float* Uj = slot(j);
-        const float* Um = slot(j - 1);
-        const float* Ua = slot(j - 2);
+        const float* Uj = slot_of(r + 2);
+        const float* Um = slot_of(r + 1);
+        const float* Ua = slot_of(r);
         const float ub = Um[oc], uc = Uj[oc], ua = Ua[oc];
         // A. fluxes of plane m = j-1
         const int m = j - 1;
@@ -308,11 +320,17 @@ __global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U
     step(Ic<0>{}, std::false_type{}, z0);
     step(Ic<1>{}, std::false_type{}, z0 + 1);
     int j = z0 + 2;
-    for (; j + 1 <= z1 + 1; j += 2) {
-        step(Ic<0>{}, std::true_type{}, j);
-        step(Ic<1>{}, std::true_type{}, j + 1);
+    for (; j + 7 <= z1 + 1; j += 8) {
+        step(Ic<2>{}, std::true_type{}, j);
+        step(Ic<3>{}, std::true_type{}, j + 1);
+        step(Ic<4>{}, std::true_type{}, j + 2);
+        step(Ic<5>{}, std::true_type{}, j + 3);
+        step(Ic<6>{}, std::true_type{}, j + 4);
+        step(Ic<7>{}, std::true_type{}, j + 5);
+        step(Ic<8>{}, std::true_type{}, j + 6);
+        step(Ic<9>{}, std::true_type{}, j + 7);
     }
-    if (j <= z1 + 1) step(Ic<0>{}, std::true_type{}, j);
+    for (; j <= z1 + 1; j++) step(j - z0, std::true_type{}, j);
     cp_async_wait<0>();
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
