@@ -401,6 +401,23 @@ int tgv_batch_run_fused(int nvol, const float* const* f, float* const* u, const 
         slots[v] = CheckSlot{V.partials, nt, V.ctl};
         ctlp[v] = V.ctl;
     }
+    // tensor maps of every volume's input arrays, per parity, when every
+    // volume qualifies for the staged pass (else the thread-loading pass runs)
+    void* d_maps = nullptr;
+    std::vector<unsigned char> maps;
+    if (tgv_tma_batch_usable(L.dims.data(), nvol)) {
+        const size_t mb = tgv_tma_maps_bytes();
+        maps.resize(mb * 2 * (size_t)nvol);
+        bool ok = true;
+        for (int v = 0; v < nvol && ok; v++)
+            for (int par = 0; par < 2 && ok; par++)
+                ok = tgv_tma_encode(vols[v].args[par], vols[v].d, maps.data() + mb * (2 * (size_t)v + par));
+        if (ok) {
+            d_maps = sc.bytes(maps.size());
+            if (!d_maps) return sc.status();
+            CILREG_CUDA(cudaMemcpyAsync(d_maps, maps.data(), maps.size(), cudaMemcpyHostToDevice, s));
+        }
+    }
     CILREG_CUDA(cudaMemcpyAsync(d_vols, vols.data(), sizeof(TgvFusedVol) * nvol, cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaMemcpyAsync(d_tile_vol, tile_vol.data(), sizeof(int) * (size_t)ntiles, cudaMemcpyHostToDevice, s));
     CILREG_CUDA(cudaMemcpyAsync(d_slots, slots.data(), sizeof(CheckSlot) * nvol, cudaMemcpyHostToDevice, s));
@@ -410,7 +427,10 @@ int tgv_batch_run_fused(int nvol, const float* const* f, float* const* u, const 
     auto enqueue = [&]() -> int {
         for (int it = 0; it < iters; it++) {
             const int check = (epsil != 0.0f && it % 5 == 0) ? 1 : 0;
-            CILREG_TRY(tgv_fused_batch_step(d_vols, d_tile_vol, ntiles, it & 1, check, s));
+            if (d_maps)
+                CILREG_TRY(tgv_tma_batch_step(d_vols, d_tile_vol, d_maps, ntiles, it & 1, check, s));
+            else
+                CILREG_TRY(tgv_fused_batch_step(d_vols, d_tile_vol, ntiles, it & 1, check, s));
             note_launch();
             if (check) CILREG_TRY(launch_finalize_batch(d_slots, nvol, epsil, it, s));
         }
@@ -425,6 +445,7 @@ int tgv_batch_run_fused(int nvol, const float* const* f, float* const* u, const 
         float* ub[2] = {u[v], ualt[v]};
         CILREG_TRY(launch_select_pingpong(d_ctl + v, iters, ub, u[v], L.dims[v].n, s));
     }
+    if (d_maps) CILREG_TRY(tgv_tma_status(s));
     return read_infos(d_ctl, nvol, infos, s);
 }
 

@@ -55,23 +55,26 @@ struct TgvMaps {
     CUtensorMap m[NA];
 };
 
-template <bool CHECK>
-__global__ void __launch_bounds__(NT, 2) k_tgv_fused_tma(const __grid_constant__ TgvMaps maps, TgvFusedArgs a,
-                                                         Dims d, int zc, const StopCtl* ctl, double2* partials) {
+// One tile (bx, by, bz) of one volume.  maps: the volume's 14 tensor maps
+// (a kernel parameter, or device memory in batched runs); A: the argument
+// block, a kernel parameter or (batched runs) a volatile copy in shared
+// memory, read at each use rather than held in registers.
+template <bool CHECK, class A>
+__device__ __forceinline__ void tma_tile(const CUtensorMap* maps, A& a, const Dims& d, int zc, int bx, int by,
+                                         int bz, float& pa_out, float& pb_out) {
     extern __shared__ unsigned char dyn[];
     __shared__ float sPQ[7][BY * BX];  // new P1, P2, Q1, Q2, Q4, Q5, Q6 of plane j
     __shared__ uint64_t bar[STAGES];
-    if (ctl->stop) return;
     float* stage0 = (float*)(((uintptr_t)dyn + 127) & ~(uintptr_t)127);
     const int tx = threadIdx.x, ty = threadIdx.y;
     const bool leader = (tx == 0 && ty == 0);
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int xf0 = blockIdx.x * OX - 1;  // x of thread tx = 0
-    const int yf0 = blockIdx.y * OY - 1;
+    const int xf0 = bx * OX - 1;  // x of thread tx = 0
+    const int yf0 = by * OY - 1;
     const int bx0 = box_x0(xf0);
     const int rx = xf0 - bx0;
     const int x = xf0 + tx, y = yf0 + ty;
-    const int z0 = blockIdx.z * zc;
+    const int z0 = bz * zc;
     const int z1 = min(z0 + zc, nz);
     const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
     const bool d_pt = in_xy && tx <= BX - 2 && ty <= BY - 2;  // dual formed here
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_fused_tma(const __grid_constant__
         const int s = p % STAGES;
         float* dst = stage0 + (size_t)s * BOX * NA;
         mbar_expect(&bar[s], STAGE_BYTES);
-        for (int q = 0; q < NA; q++) load_box(dst + q * BOX, &maps.m[q], bx0, yf0, z0 - 1 + p, &bar[s]);
+        for (int q = 0; q < NA; q++) load_box(dst + q * BOX, maps + q, bx0, yf0, z0 - 1 + p, &bar[s]);
     };
     if (leader)
         for (int p = 0; p < STAGES && p < nplanes; p++) issue(p);
@@ -185,7 +188,41 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_fused_tma(const __grid_constant__
         zq5 = n.q5;
         zq6 = n.q6;
     }
+    pa_out = pa;
+    pb_out = pb;
+}
+
+template <bool CHECK>
+__global__ void __launch_bounds__(NT, 2) k_tgv_fused_tma(const __grid_constant__ TgvMaps maps, TgvFusedArgs a,
+                                                         Dims d, int zc, const StopCtl* ctl, double2* partials) {
+    if (ctl->stop) return;
+    float pa = 0.f, pb = 0.f;
+    tma_tile<CHECK, TgvFusedArgs>(maps.m, a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+}
+
+// one iteration of every volume of a batch: a flat grid over all volumes'
+// tiles; `parity` selects the (old, new) buffer pair of the iteration and the
+// tensor maps of its old buffers (maps + (2 v + parity) x 14 for volume v)
+template <bool CHECK>
+__global__ void __launch_bounds__(NT, 2) k_tgv_fused_tma_batch(const TgvFusedVol* __restrict__ vols,
+                                                               const int* __restrict__ tile_vol,
+                                                               const CUtensorMap* __restrict__ maps, int parity) {
+    __shared__ TgvFusedArgs sa;
+    const long long t = blockIdx.x;
+    const int v = tile_vol[t];
+    const TgvFusedVol& V = vols[v];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    const int bx = (int)(lt % V.gx);
+    const int by = (int)((lt / V.gx) % V.gy);
+    const int bz = (int)(lt / ((long long)V.gx * V.gy));
+    if (threadIdx.x == 0 && threadIdx.y == 0) sa = V.args[parity];
+    __syncthreads();
+    volatile TgvFusedArgs& va = sa;
+    float pa = 0.f, pb = 0.f;
+    tma_tile<CHECK, volatile TgvFusedArgs>(maps + ((size_t)v * 2 + parity) * NA, va, V.d, V.zc, bx, by, bz, pa, pb);
+    if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
 }
 
 template <bool CHECK>
@@ -193,7 +230,9 @@ bool raise_smem_limit() {
     static const bool ok = [] {
         const bool r =
             cudaFuncSetAttribute(k_tgv_fused_tma<CHECK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN) ==
-            cudaSuccess;
+                cudaSuccess &&
+            cudaFuncSetAttribute(k_tgv_fused_tma_batch<CHECK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)DYN) == cudaSuccess;
         cudaGetLastError();
         return r;
     }();
@@ -210,14 +249,40 @@ bool tgv_tma_usable(const Dims& d) {
 
 int tgv_tma_resident() {
     static const int r = [] {
-        int n = 0;
+        int n = 0, nb = 0;
         if (!raise_smem_limit<false>() || !raise_smem_limit<true>() ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tgv_fused_tma<false>, NT, DYN) != cudaSuccess)
-            n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tgv_fused_tma<false>, NT, DYN) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tgv_fused_tma_batch<false>, NT, DYN) !=
+                cudaSuccess)
+            n = nb = 0;
         cudaGetLastError();
-        return n;
+        return n < nb ? n : nb;
     }();
     return r;
+}
+
+bool tgv_tma_batch_usable(const Dims* dims, int nvol) {
+    const char* e = getenv("CILREG_TGV_TMA");
+    if (e && e[0] == '0') return false;
+    for (int v = 0; v < nvol; v++)
+        if (!tma::volume_ok(dims[v]) || dims[v].n >= (1LL << 31)) return false;
+    return tgv_tma_resident() >= 2;
+}
+
+int tgv_tma_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, const void* d_maps, long long ntiles,
+                       int parity, int check, cudaStream_t s) {
+    if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    if (!raise_smem_limit<false>() || !raise_smem_limit<true>())
+        return fail(ERR_CUDA, __FILE__, __LINE__, "cannot raise the shared-memory limit of k_tgv_fused_tma_batch");
+    const CUtensorMap* maps = (const CUtensorMap*)d_maps;
+    if (check)
+        k_tgv_fused_tma_batch<true><<<dim3((unsigned)ntiles), dim3(BX, BY, 1), DYN, s>>>(d_vols, d_tile_vol, maps,
+                                                                                         parity);
+    else
+        k_tgv_fused_tma_batch<false><<<dim3((unsigned)ntiles), dim3(BX, BY, 1), DYN, s>>>(d_vols, d_tile_vol, maps,
+                                                                                          parity);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
 }
 
 size_t tgv_tma_maps_bytes() { return sizeof(TgvMaps); }

@@ -69,6 +69,13 @@ int tgv_tma_step(const TgvPlan& T, const void* maps, const TgvFusedArgs& a, cons
                  int check, double2* partials, cudaStream_t s);
 // fails if a tensor-copy wait of the staged kernel ran out (and clears the flag)
 int tgv_tma_status(cudaStream_t s);
+// batched runs of the staged pass: every volume qualifies (x extent a
+// multiple of 4, below 2^31 voxels); d_maps holds, for volume v and parity
+// p, the maps of args[p]'s input arrays at d_maps + (2 v + p) x
+// tgv_tma_maps_bytes()
+bool tgv_tma_batch_usable(const Dims* dims, int nvol);
+int tgv_tma_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, const void* d_maps, long long ntiles,
+                       int parity, int check, cudaStream_t s);
 
 // tiling of the streaming primal kernel in a batched run (64-plane chunks)
 void tgv_primal_tiles(const Dims& d, int& gx, int& gy, int& gz, int& zc);

@@ -55,6 +55,33 @@ def test_tgv_batch_equals_single_calls(shapes, epsil):
         assert np.max(np.abs(o - ref)) <= rel_tol(ref, 1e-6)
 
 
+SHAPES_3D_X4 = [(17, 30, 40), (64, 33, 20), (9, 9, 72), (40, 40, 40), (3, 200, 32), (70, 12, 4)]
+
+
+@pytest.mark.parametrize("epsil", [0.0, 3e-3])
+def test_tgv_batch_with_tensor_copy_staging(epsil, monkeypatch):
+    """Every x extent a multiple of 4: the batch stages its inputs by tensor
+    copies and agrees with the thread-loading batch and with single calls
+    (the same stopping iterations)."""
+    from ccpi.filters.batch import TGV_batch
+    from ccpi.filters.regularisers import TGV
+
+    vols = _volumes(SHAPES_3D_X4, 8)
+    infos = np.zeros((len(vols), 2), np.float32)
+    outs = TGV_batch(vols, 0.05, 1.0, 2.0, 40, 12.0, epsil, infovectors=infos)
+    monkeypatch.setenv("CILREG_TGV_TMA", "0")
+    infos0 = np.zeros((len(vols), 2), np.float32)
+    outs0 = TGV_batch(vols, 0.05, 1.0, 2.0, 40, 12.0, epsil, infovectors=infos0)
+    monkeypatch.delenv("CILREG_TGV_TMA")
+    np.testing.assert_array_equal(infos[:, 0], infos0[:, 0])
+    for v, o, o0, inf in zip(vols, outs, outs0, infos):
+        assert np.max(np.abs(o - o0)) <= rel_tol(o0, 1e-6)
+        ref_info = np.zeros(2, np.float32)
+        ref = TGV(v, 0.05, 1.0, 2.0, 40, 12.0, epsil, device="gpu", infovector=ref_info)
+        assert int(inf[0]) == int(ref_info[0])
+        assert np.max(np.abs(o - ref)) <= rel_tol(ref, 1e-6)
+
+
 def test_fgp_batch_autotuned_chunks(monkeypatch, tmp_path):
     """Any z chunk the autotuner picks computes the same iteration."""
     import torch
