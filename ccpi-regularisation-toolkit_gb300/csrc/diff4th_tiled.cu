@@ -3,9 +3,9 @@
 //
 // The update needs the weighted Laplacian W at the voxel and its mirrored
 // neighbours; W needs U on the mirrored 19-point neighbourhood.  A CTA of
-// 32 x 16 threads holds an overlapping tile (thread (tx, ty) on voxel
-// (x0 - 2 + tx, y0 - 2 + ty)); W is formed on the inner 30 x 14 voxels, the
-// update on the inner 28 x 12.  Step j of each thread:
+// 32 x 24 threads holds an overlapping tile (thread (tx, ty) on voxel
+// (x0 - 2 + tx, y0 - 2 + ty)); W is formed on the inner 30 x 22 voxels, the
+// update on the inner 28 x 20.  Step j of each thread:
 //   B. publishes U(j) into a four-plane shared-memory ring;
 //   A. after the barrier, forms W(j-1) once per voxel from planes j-2, j-1, j
 //      of the ring (mirrored in all three axes) into shared memory;
@@ -13,8 +13,9 @@
 //      x/y from shared memory).
 // One barrier per plane.  HBM traffic: read U and f, write U (12 B/voxel);
 // the reference's two sweeps move 24 B and store W.  The kernel is bound by
-// instruction issue and latency: at 40 registers three CTAs fit on an SM
-// (1.41 -> 1.31 ms per 512^3 iteration against two CTAs at 56 registers).
+// instruction issue and latency: at 40 registers two 768-thread CTAs (48
+// warps) fit on an SM.  The 24-row tile spends 1.37 thread-steps per updated
+// voxel against 1.52 for 16 rows (1.30 -> 1.26 ms per 512^3 iteration).
 #include <type_traits>
 
 #include "diff4th_tiled.cuh"
@@ -23,7 +24,7 @@ namespace cilreg {
 
 namespace {
 
-constexpr int BX = 32, BY = 16;
+constexpr int BX = 32, BY = 24;
 constexpr int OX = BX - 4, OY = BY - 4;
 constexpr int NT = BX * BY;
 constexpr int ZCHUNK = 64;
@@ -34,7 +35,7 @@ using Ic = std::integral_constant<int, V>;
 // CHECK: a stopping-check iteration (per-CTA partial sums).  IT: element-offset
 // type (int below 2^31 voxels).
 template <bool THREE, bool CHECK, typename IT>
-__global__ void __launch_bounds__(NT, 3) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
+__global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                      const float* __restrict__ F, float lam, float tau, float isg2,
                                                      Dims d, int zc, const StopCtl* ctl, double2* partials) {
     __shared__ float sU[4][BY][BX];
