@@ -261,6 +261,12 @@ long long cilreg_launch_count(void);
  * pool holds unused (for callers that share the device with another
  * allocator).  0 or a negative status. */
 int cilreg_release_cached(int gpu_device);
+/* Self-test of the bounded waits of the kernels that stage their inputs by
+ * tensor copies: one CTA waits on an mbarrier whose 16 expected bytes never
+ * arrive (no copy is issued).  *ran_out = 1 when the wait gave up after its
+ * try limit, as it must, and the device then still ran a kernel.  0 or a
+ * negative status. */
+int cilreg_selftest_wait_limit(int gpu_device, int *ran_out);
 
 #ifdef __cplusplus
 }
