@@ -12,6 +12,11 @@ from __future__ import annotations
 SHAPE_2D = (40, 56)       # (Y, X)
 SHAPE_3D = (10, 16, 22)   # (Z, Y, X)
 SEEDS = {2: (6, 11), 3: (8, 12)}  # (number of shapes, seed)
+# a second 3D input whose x extent is a multiple of 4, the volumes the kernels
+# that stage their inputs by tensor copies run on (FGP, TGV)
+SHAPE_3D_X4 = (10, 16, 24)
+SEED_3D_X4 = (8, 13)
+STAGED = ("fgp_iso", "fgp_aniso_nonneg", "fgp_stop", "tgv", "tgv_stop")
 
 
 def _c(name, alg, **p):
@@ -64,11 +69,30 @@ def cases():
     return out
 
 
+def staged_cases():
+    """The FGP and TGV cases on the 3D input of x extent 24 (key suffix 3dx4)."""
+    out = []
+    for c in _BASE:
+        if c["name"] in STAGED:
+            d = dict(c)
+            d["dim"] = 3
+            d["key"] = f"{c['name']}_3dx4"
+            out.append(d)
+    return out
+
+
 def make_input(dim: int):
     from ccpi.supp.phantoms import noisy_phantom
 
     n, seed = SEEDS[dim]
     return noisy_phantom(SHAPE_2D if dim == 2 else SHAPE_3D, n, seed)
+
+
+def make_input_x4():
+    from ccpi.supp.phantoms import noisy_phantom
+
+    n, seed = SEED_3D_X4
+    return noisy_phantom(SHAPE_3D_X4, n, seed)
 
 
 def make_ref(dim: int, shape=None):

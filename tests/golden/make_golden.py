@@ -3,7 +3,8 @@
 Runs every case of ``cases.py`` through ``oracle/_ref/libcilreg_ref.so`` (the
 reference sources compiled by ``make -C oracle ref``) and stores inputs (and
 the FGP-dTV reference images), outputs, infovectors and TV energies in
-``reference_outputs.npz``.  The reference's
+``reference_outputs.npz``; also the FGP and TGV cases on a second 3D input
+whose x extent is a multiple of 4 (``staged_cases``).  The reference's
 non-linear diffusion updates in place, so it is run with one OpenMP thread
 (lexicographic order), the only deterministic setting.
 
@@ -42,6 +43,12 @@ def main():
     for case in C.cases():
         x = arrays[f"input_{case['dim']}d"]
         out, info = C.run_oracle(case, x, use_ref=True, ref=arrays[f"ref_{case['dim']}d"])
+        arrays[f"out_{case['key']}"] = out
+        arrays[f"info_{case['key']}"] = info
+        print(f"{case['key']:24s} iters={int(info[0]):4d} re={info[1]:.3e}")
+    arrays["input_3dx4"] = C.make_input_x4()
+    for case in C.staged_cases():
+        out, info = C.run_oracle(case, arrays["input_3dx4"], use_ref=True)
         arrays[f"out_{case['key']}"] = out
         arrays[f"info_{case['key']}"] = info
         print(f"{case['key']:24s} iters={int(info[0]):4d} re={info[1]:.3e}")

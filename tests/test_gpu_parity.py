@@ -57,6 +57,23 @@ def test_gpu_matches_reference(case, golden):
         assert abs(float(info[1]) - float(ref_info[1])) <= 1e-2 * float(ref_info[1]) + 1e-9
 
 
+@pytest.mark.parametrize("case", C.staged_cases(), ids=lambda c: c["key"])
+def test_staged_kernels_match_reference(case, golden, monkeypatch):
+    """x extent a multiple of 4: the FGP iteration staged by tensor copies
+    (forced at this size) and the TGV iteration staged by tensor copies (the
+    default) against the reference's own outputs."""
+    monkeypatch.setenv("CILREG_FGP_TMA", "1")
+    x = golden["input_3dx4"]
+    out, info = C.run_gpu(case, x, api="gpu")
+    ref = golden[f"out_{case['key']}"]
+    ref_info = golden[f"info_{case['key']}"]
+    if int(info[0]) != int(ref_info[0]):
+        assert _borderline(case, x), f"stopping iteration {int(info[0])} != reference {int(ref_info[0])}"
+        pytest.skip("borderline stopping check (a relative change within 2% of epsil)")
+    err = float(np.max(np.abs(out - ref)))
+    assert err <= rel_tol(ref, TOL), f"max abs err {err:.3e} > {rel_tol(ref, TOL):.3e}"
+
+
 SUBSET = [c for c in C.cases() if c["name"] in ("rof", "fgp_stop", "pd_stop", "sb_iso", "tgv", "ndf_huber", "d4")]
 
 

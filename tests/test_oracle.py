@@ -34,6 +34,21 @@ def test_port_matches_reference_fixture(case, golden):
 def test_fixture_inputs_are_the_seeded_phantoms(golden):
     for dim in (2, 3):
         np.testing.assert_array_equal(C.make_input(dim), golden[f"input_{dim}d"])
+    np.testing.assert_array_equal(C.make_input_x4(), golden["input_3dx4"])
+
+
+@pytest.mark.parametrize("case", C.staged_cases(), ids=lambda c: c["key"])
+def test_port_matches_reference_fixture_x4(case, golden):
+    """The FGP and TGV cases on the 3D input whose x extent is a multiple of 4."""
+    x = golden["input_3dx4"]
+    out, info = C.run_oracle(case, x, use_ref=False, jacobi=False)
+    ref = golden[f"out_{case['key']}"]
+    ref_info = golden[f"info_{case['key']}"]
+    assert int(info[0]) == int(ref_info[0])
+    if _bit_exact_platform():
+        np.testing.assert_array_equal(out, ref)
+    else:
+        assert np.max(np.abs(out - ref)) <= rel_tol(ref, 1e-6)
 
 
 ODD_SHAPES = [(3, 5), (7, 2), (2, 3, 5), (5, 4, 3), (13, 9, 2)]
