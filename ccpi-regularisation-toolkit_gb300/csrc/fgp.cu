@@ -150,9 +150,9 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
         const size_t mb = fgp_tma_maps_bytes();
         maps.resize(mb * R);
         for (int r = 0; r < R && tma; r++) {
-            const float* arr[8] = {ring[(r + R - 1) % R][0], ring[(r + R - 1) % R][1], ring[(r + R - 1) % R][2],
+            const float* arr[7] = {ring[(r + R - 1) % R][0], ring[(r + R - 1) % R][1], ring[(r + R - 1) % R][2],
                                    ring[(r + R - 2) % R][0], ring[(r + R - 2) % R][1], ring[(r + R - 2) % R][2],
-                                   f, u_out};
+                                   f};
             tma = fgp_tma_encode(arr, d, maps.data() + mb * r);
         }
     }

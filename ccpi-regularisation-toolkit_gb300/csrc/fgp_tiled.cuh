@@ -47,10 +47,10 @@ int fgp_pair_step(const PairPlan& T, const float* const pc[3], const float* cons
 // The iteration with tensor-copy (TMA) staging of its inputs (fgp_tma.cu):
 // 3D, x extent a multiple of 4, below 2^31 voxels; CILREG_FGP_TMA=0 turns it off.
 bool fgp_tma_usable(const Dims& d);
-// tensor maps of the eight inputs (pc[0..2], po[0..2], f, U) into `maps_out`
+// tensor maps of the seven staged inputs (pc[0..2], po[0..2], f) into `maps_out`
 // (fgp_tma_maps_bytes() bytes); false when an array is not 16-byte aligned or
 // the driver refuses the map
-bool fgp_tma_encode(const float* const arrays[8], const Dims& d, void* maps_out);
+bool fgp_tma_encode(const float* const arrays[7], const Dims& d, void* maps_out);
 size_t fgp_tma_maps_bytes();
 // CTAs of the tensor-copy kernel resident per SM
 int fgp_tma_resident();

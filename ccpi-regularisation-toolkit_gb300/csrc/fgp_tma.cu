@@ -9,7 +9,9 @@
 // (cp.async.bulk.tensor) of the tile's box per plane into a ring of STAGES
 // shared-memory stages, STAGES - 1 planes ahead, completing on one mbarrier
 // per stage; every thread then reads its own voxel's values from the stage.
-// A stopping-check iteration stages U_prev the same way (an eighth array).
+// A stopping-check iteration also reads U_prev at each thread's own voxel,
+// by plain loads one plane ahead (staging it as an eighth array would leave
+// only three CTAs per SM).
 // The box is 36 x 16 voxels starting at the tile's first x rounded down to a
 // multiple of 4 (a tensor copy's x origin must be 16-byte aligned), and the
 // thread reads column tx + r; voxels outside the volume (also planes below 0
@@ -32,12 +34,12 @@ constexpr int BX = 32, BY = 16;          // threads
 constexpr int OX = BX - 2, OY = BY - 2;  // output voxels per tile
 constexpr int NT = BX * BY;
 constexpr int BOX = BOXX * BY;           // floats per array per stage
-constexpr int NIN = 8;                   // pc (3), po (3), f, and U_prev on check iterations
+constexpr int NIN = 7;                   // pc (3), po (3), f
 // arrays staged (7, or 8 on check iterations) and ring depth (planes in
 // flight + 1) per variant
 template <bool CHECK, int ST>
 struct Ring {
-    static constexpr int NA = CHECK ? 8 : 7;
+    static constexpr int NA = 7;  // U_prev (check iterations) is loaded by the threads
     static constexpr int STAGES = ST;
     static constexpr size_t DYN = sizeof(float) * BOX * NA * STAGES + 128;  // + alignment slack
 };
@@ -52,11 +54,11 @@ struct TmaArgs {
 };
 
 struct TmaMaps {
-    CUtensorMap m[NIN];  // pc[0..2], po[0..2], f, U
+    CUtensorMap m[NIN];  // pc[0..2], po[0..2], f
 };
 
 template <bool CHECK, int ST>
-__global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMaps maps, TmaArgs a, Dims d, int zc,
+__global__ void __launch_bounds__(NT, CHECK ? 4 : 3) k_fgp_tma(const __grid_constant__ TmaMaps maps, TmaArgs a, Dims d, int zc,
                                                    const StopCtl* ctl, double2* partials) {
     extern __shared__ unsigned char dyn[];
     __shared__ float sR1[BY][BX];
@@ -119,8 +121,11 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_tma(const __grid_constant__ TmaMa
         const float r1 = c1 + a.c * (c1 - o1);
         const float r2 = c2 + a.c * (c2 - o2);
         const float r3 = c3 + a.c * (c3 - o3);
-        // U_prev of plane k (check iterations), consumed one plane later
-        const float uo_next = CHECK ? st[7 * BOX] : 0.f;
+        // U_prev of plane k (check iterations; the voxel's own value, written by
+        // the previous iteration), loaded one plane before it is consumed: a
+        // plain load, not a staged box, so that the check variant needs the
+        // plain one's shared memory and four CTAs still fit on an SM
+        const float uo_next = (CHECK && p_pt && k >= z0 && k < z1) ? a.u[k * sxy + col] : 0.f;
         sR1[ty][tx] = r1;
         sR2[ty][tx] = r2;
         __syncthreads();
@@ -193,7 +198,7 @@ bool fgp_tma_usable(const Dims& d) {
     return tma::volume_ok(d) && d.n >= min_n && d.n < (1LL << 31);
 }
 
-bool fgp_tma_encode(const float* const arrays[8], const Dims& d, void* maps_out) {
+bool fgp_tma_encode(const float* const arrays[7], const Dims& d, void* maps_out) {
     TmaMaps* M = (TmaMaps*)maps_out;
     for (int q = 0; q < NIN; q++)
         if (!tma::encode(&M->m[q], arrays[q], d, BY)) return false;
