@@ -38,6 +38,8 @@ template <bool THREE, bool CHECK, typename IT>
 __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U, float* __restrict__ Un,
                                                      const float* __restrict__ F, float lam, float tau, float isg2,
                                                      Dims d, int zc, const StopCtl* ctl, double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     __shared__ float sU[4][BY][BX];
     __shared__ float sW[2][BY][BX];
     if (ctl->stop) return;
@@ -191,8 +193,7 @@ int d4_stream_step(const D4Plan& T, const float* cur, float* nxt, const float* f
     else
         kern = three ? (check ? k_d4_stream<true, true, long long> : k_d4_stream<true, false, long long>)
                      : (check ? k_d4_stream<false, true, long long> : k_d4_stream<false, false, long long>);
-    kern<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, partials));
     return OK;
 }
 

@@ -197,6 +197,8 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
 template <bool THREE, bool CHECK, typename IT, bool DTV = false>
 __global__ void __launch_bounds__(NT, DTV ? 2 : 3) k_fgp_stream(TiledArgs a, Dims d, int zc, const StopCtl* ctl,
                                                                 double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     if (ctl->stop) return;
     float pa = 0.f, pb = 0.f;
     fgp_stream_tile<THREE, CHECK, IT, DTV>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
@@ -336,8 +338,7 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
     else
         kern = three ? (check ? k_fgp_stream<true, true, long long> : k_fgp_stream<true, false, long long>)
                      : (check ? k_fgp_stream<false, true, long long> : k_fgp_stream<false, false, long long>);
-    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }
 

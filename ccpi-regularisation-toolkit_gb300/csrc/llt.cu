@@ -52,6 +52,8 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
                                                       const float* __restrict__ F, float lam_rof, float lam_llt,
                                                       float tau, Dims d, int zc, const StopCtl* ctl,
                                                       double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     __shared__ float sU[4][BY * BX];
     __shared__ float sR1[2][BY * BX];  // ROF D1 (j axis), read at j-1
     __shared__ float sR2[2][BY * BX];  // ROF D2 (i axis), read at i-1
@@ -218,9 +220,8 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
         // small volume, fixed count: launch overhead dominates, replay a graph
         auto kern = three ? k_llt_stream<true, false, int> : k_llt_stream<false, false, int>;
         CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
-            kern<<<T.grid, T.block, 0, st>>>(bufs[k & 1], bufs[(k + 1) & 1], f, lam_rof, lam_llt, tau, d, T.zchunk,
-                                             ctl.ctl(), ctl.partials());
-            CILREG_CUDA(cudaGetLastError());
+            CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, st, (const float*)bufs[k & 1], bufs[(k + 1) & 1], f,
+                                   lam_rof, lam_llt, tau, d, T.zchunk, (const StopCtl*)ctl.ctl(), ctl.partials()));
             note_launch();
             return OK;
         }));
@@ -235,9 +236,8 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
         else
             kern = three ? (check ? k_llt_stream<true, true, long long> : k_llt_stream<true, false, long long>)
                          : (check ? k_llt_stream<false, true, long long> : k_llt_stream<false, false, long long>);
-        kern<<<T.grid, T.block, 0, s>>>(bufs[it & 1], bufs[(it + 1) & 1], f, lam_rof, lam_llt, tau, d, T.zchunk,
-                                        ctl.ctl(), ctl.partials());
-        CILREG_CUDA(cudaGetLastError());
+        CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, (const float*)bufs[it & 1], bufs[(it + 1) & 1], f,
+                               lam_rof, lam_llt, tau, d, T.zchunk, (const StopCtl*)ctl.ctl(), ctl.partials()));
         note_launch();
         if (check) {
             CILREG_TRY(ctl.after_check(it, T.nblocks));

@@ -45,6 +45,8 @@ __global__ void __launch_bounds__(NT, 3) k_ndf_stream(const float* __restrict__ 
     __shared__ float sU[2][BY * BX];
     __shared__ float sFx[2][BY * BX];
     __shared__ float sFy[2][BY * BX];
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     if (ctl->stop) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -157,13 +159,12 @@ __global__ void __launch_bounds__(NT, 3) k_ndf_stream(const float* __restrict__ 
 }
 
 template <bool THREE, bool CHECK>
-void launch(int pen, const NdfPlan& T, cudaStream_t s, const float* cur, float* nxt, const float* f, float lam,
-            float sg, float isg, float tau, const Dims& d, const StopCtl* ctl, double2* part) {
-#define NDF_STREAM_CASE(P)                                                                                   \
-    case P:                                                                                                  \
-        k_ndf_stream<THREE, P, CHECK><<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam, sg, isg, tau, d, T.zchunk, \
-                                                                  ctl, part);                                \
-        break;
+cudaError_t launch(int pen, const NdfPlan& T, cudaStream_t s, const float* cur, float* nxt, const float* f,
+                   float lam, float sg, float isg, float tau, const Dims& d, const StopCtl* ctl, double2* part) {
+#define NDF_STREAM_CASE(P) \
+    case P:                \
+        return launch_pdl(k_ndf_stream<THREE, P, CHECK>, T.grid, T.block, 0, s, cur, nxt, f, lam, sg, isg, tau, d, \
+                          T.zchunk, ctl, part);
     switch (pen) {
         NDF_STREAM_CASE(0)
         NDF_STREAM_CASE(1)
@@ -174,6 +175,7 @@ void launch(int pen, const NdfPlan& T, cudaStream_t s, const float* cur, float* 
         default: break;
     }
 #undef NDF_STREAM_CASE
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -202,16 +204,15 @@ int ndf_stream_step(const NdfPlan& T, int pen, const float* cur, float* nxt, con
                     cudaStream_t s) {
     if (d.nz > 1) {
         if (check)
-            launch<true, true>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials);
+            CILREG_CUDA((launch<true, true>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials)));
         else
-            launch<true, false>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials);
+            CILREG_CUDA((launch<true, false>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials)));
     } else {
         if (check)
-            launch<false, true>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials);
+            CILREG_CUDA((launch<false, true>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials)));
         else
-            launch<false, false>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials);
+            CILREG_CUDA((launch<false, false>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials)));
     }
-    CILREG_CUDA(cudaGetLastError());
     return OK;
 }
 

@@ -34,6 +34,8 @@ __global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int
     __shared__ float sUe[2][BY][BX];
     __shared__ float sP1[2][BY][BX];
     __shared__ float sP2[2][BY][BX];
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     if (ctl->stop) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -161,8 +163,7 @@ int pd_stream_step(const PdPlan& T, const PdStreamArgs& a, const Dims& d, const 
     else
         kern = three ? (check ? k_pd_stream<true, true, long long> : k_pd_stream<true, false, long long>)
                      : (check ? k_pd_stream<false, true, long long> : k_pd_stream<false, false, long long>);
-    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }
 

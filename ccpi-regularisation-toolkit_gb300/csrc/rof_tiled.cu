@@ -74,7 +74,6 @@ __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ 
     __shared__ float sU[2][BY * BX];
     __shared__ float sD1[2][BY * BX];
     __shared__ float sD2[2][BY * BX];
-    if (ctl->stop) return;
     const float EPS = 1.0e-8f;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -99,12 +98,22 @@ __global__ void __launch_bounds__(NT, 3) k_rof_stream(const float* __restrict__ 
     // fluxes are never read), so loads need no predicate
     const IT col = (IT)min(max(y, 0), ny - 1) * nx + min(max(x, 0), nx - 1);
     float pa = 0.f, pb = 0.f;
+    // f and the lambda map never change during a run: in a plane they are
+    // loaded before waiting for the previous iteration (launch_pdl)
+    float fv0 = 0.f, lv0 = lam;
+    if constexpr (!THREE) {
+        fv0 = o_pt ? __ldg(F + col) : 0.f;
+        lv0 = (LARR && o_pt) ? __ldg(lam_arr + col) : lam;
+    }
+    pdl_wait();  // the previous iteration has completed and its writes are visible
+    pdl_trigger();
+    if (ctl->stop) return;
 
     if constexpr (!THREE) {
         // one plane: publish U, form D1/D2, update
         const float u = __ldg(U + col);
-        const float fv = o_pt ? __ldg(F + col) : 0.f;
-        const float lv = (LARR && o_pt) ? __ldg(lam_arr + col) : lam;
+        const float fv = fv0;
+        const float lv = lv0;
         sU[0][oc] = u;
         __syncthreads();
         const float xp = sU[0][oxh] - u, xm = u - sU[0][oxl];
@@ -223,6 +232,8 @@ __global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U
                                                      const float* __restrict__ F, const float* __restrict__ lam_arr,
                                                      float lam, float tau, Dims d, int zc, const StopCtl* ctl,
                                                      double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     __shared__ float sU[RING][BY * BX];
     __shared__ float sD1[2][BY * BX];
     __shared__ float sD2[2][BY * BX];
@@ -361,8 +372,7 @@ int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* 
         // CILREG_ROF_KERNEL=reg keeps the register-pipelined kernel (A/B checks)
         auto ka = check ? (larr ? k_rof_async<true, true, int> : k_rof_async<true, false, int>)
                         : (larr ? k_rof_async<false, true, int> : k_rof_async<false, false, int>);
-        ka<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials);
-        CILREG_CUDA(cudaGetLastError());
+        CILREG_CUDA(launch_pdl(ka, T.grid, T.block, 0, s, cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials));
         return OK;
     }
     decltype(&k_rof_stream<true, true, true, int>) kern;
@@ -377,8 +387,7 @@ int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* 
                      : (check ? (larr ? k_rof_stream<false, true, true, long long> : k_rof_stream<false, true, false, long long>)
                               : (larr ? k_rof_stream<false, false, true, long long> : k_rof_stream<false, false, false, long long>));
     }
-    kern<<<T.grid, T.block, 0, s>>>(cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, cur, nxt, f, lam_arr, lam, tau, d, T.zchunk, ctl, partials));
     return OK;
 }
 

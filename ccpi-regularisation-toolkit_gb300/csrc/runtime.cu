@@ -95,6 +95,11 @@ int sm_count() {
     return n;
 }
 
+bool pdl_enabled() {
+    const char* e = getenv("CILREG_PDL");
+    return !(e && e[0] == '0');
+}
+
 int wave_zchunk(long long tiles_xy, int nz, int resident, int extra, int max_chunk) {
     if (nz <= 1) return 1;
     if (max_chunk > nz) max_chunk = nz;

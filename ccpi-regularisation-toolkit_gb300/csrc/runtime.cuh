@@ -137,6 +137,40 @@ struct NoTail {
 template <class Enq, class Tail = NoTail>
 int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue, Tail tail = Tail());
 
+// Programmatic dependent launch: an iteration kernel launched with
+// launch_pdl may be scheduled while the kernel before it in the stream is
+// still draining; it runs pdl_wait() before its first memory access (the
+// previous grid has then completed and its writes are visible, so both the
+// read-after-write and the write-after-read order of ping-pong buffers hold)
+// and pdl_trigger() to let its own successor be scheduled early.  Both
+// instructions do nothing in a kernel launched without the attribute.
+// CILREG_PDL=0 launches normally (A/B checks).  launch_pdl returns the launch
+// status and clears it from the thread's error state.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args... args) {
+    if (!pdl_enabled()) {
+        kernel<<<grid, block, smem, s>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, ((KArgs)args)...);
+    cudaGetLastError();  // the status is returned; leave no stale error behind
+    return e;
+}
+
 // process-wide count of kernels this library has launched (for benchmarks)
 void note_launch(long long n = 1);
 long long launch_count();

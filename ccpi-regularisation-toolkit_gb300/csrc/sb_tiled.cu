@@ -36,6 +36,8 @@ using Ic = std::integral_constant<int, V>;
 template <bool THREE, bool CHECK>
 __global__ void __launch_bounds__(NT, 2) k_sb_sweep2(SbSweepArgs a, Dims d, int zc, const StopCtl* ctl,
                                                      double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     __shared__ float sU0[2][BY * BX];
     __shared__ float sU1[2][BY * BX];
     __shared__ float sDx[2][BY * BX];
@@ -237,6 +239,8 @@ __device__ __forceinline__ void sb_shrink(float g1, float g2, float g3, float b1
 template <bool THREE, bool CHECK, bool ANISO>
 __global__ void __launch_bounds__(NT, 2) k_sb_fused(SbFusedArgs a, Dims d, int zc, const StopCtl* ctl,
                                                     double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     __shared__ float sU0[4][BY * BX];
     __shared__ float sU1[2][BY * BX];
     __shared__ float sDx[2][BY * BX];
@@ -448,8 +452,7 @@ int sb_sweep2_step(const SbPlan& T, const SbSweepArgs& a, const Dims& d, const S
     const bool three = d.nz > 1;
     auto kern = three ? (check ? k_sb_sweep2<true, true> : k_sb_sweep2<true, false>)
                       : (check ? k_sb_sweep2<false, true> : k_sb_sweep2<false, false>);
-    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }
 
@@ -467,8 +470,7 @@ int sb_fused_step(const SbPlan& T, const SbFusedArgs& a, bool aniso, const Dims&
     else
         kern = check ? (aniso ? k_sb_fused<false, true, true> : k_sb_fused<false, true, false>)
                      : (aniso ? k_sb_fused<false, false, true> : k_sb_fused<false, false, false>);
-    kern<<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }
 

@@ -148,6 +148,8 @@ __device__ __forceinline__ void fused_tile(A& a, const Dims& d, int zc, int bx, 
 template <bool CHECK>
 __global__ void __launch_bounds__(NT, 2) k_tgv_fused(TgvFusedArgs a, Dims d, int zc, const StopCtl* ctl,
                                                      double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
     if (ctl->stop) return;
     float pa = 0.f, pb = 0.f;
     fused_tile<CHECK, const TgvFusedArgs>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
@@ -213,10 +215,9 @@ int tgv_fused_batch_step(const TgvFusedVol* d_vols, const int* d_tile_vol, long 
 int tgv_fused_step(const TgvPlan& T, const TgvFusedArgs& a, const Dims& d, const StopCtl* ctl, int check,
                    double2* partials, cudaStream_t s) {
     if (check)
-        k_tgv_fused<true><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
+        CILREG_CUDA(launch_pdl(k_tgv_fused<true>, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     else
-        k_tgv_fused<false><<<T.grid, T.block, 0, s>>>(a, d, T.zchunk, ctl, partials);
-    CILREG_CUDA(cudaGetLastError());
+        CILREG_CUDA(launch_pdl(k_tgv_fused<false>, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }
 
