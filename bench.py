@@ -144,12 +144,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(x, iters, use_threads=None):
-    """Reference C-OMP FGP on the host (compiled reference if loadable here, else the port)."""
+def host_info():
+    """CPU model and logical core count of this host (recorded beside every CPU figure)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return {"cpu_model": model or platform.processor() or platform.machine(), "nproc": os.cpu_count()}
+
+
+def cpu_baseline(x, iters):
+    """Reference C-OMP FGP on the host: the reference's own sources compiled on
+    this machine (oracle/_ref) when they were staged, else the oracle's C
+    restatement, with OpenMP on every host core."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     kind = "reference" if O.ref_lib() is not None else "port"
     t = time.perf_counter()
     O.fgp_tv(x, LAM, iters, 0.0, METHOD, NONNEG, use_ref=(kind == "reference"))
@@ -159,26 +177,32 @@ def cpu_baseline(x, iters, use_threads=None):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU implementation of the path
+    (TV_FGP_CPU_main, FGP_TV_core.c:40) on every host core, each step a fixed
+    sample of --ref-iters iterations of the benchmark volume (epsil 0: the
+    per-iteration cost is constant), reported as voxel-iterations/s."""
     rank, world, _ = _env_rank()
     if rank != 0:
         return 0
     x = _phantom(args.size)
     iters = args.ref_iters
     for _ in range(args.warmup):
-        cpu_baseline(x, iters)
-    vals, kind, cores, secs = [], None, None, 0.0
+        cpu_baseline(x, 1)
+    kind, cores, secs = None, None, 0.0
     for _ in range(args.steps):
-        v, kind, cores, dt = cpu_baseline(x, iters)
-        vals.append(v)
+        _, kind, cores, dt = cpu_baseline(x, iters)
         secs += dt
     value = x.size * iters * args.steps / secs
-    sample = f"FGP_TV {args.size}^3, {iters} fixed iterations per step (epsil=0), iso, nonneg"
+    sample = (f"FGP_TV {args.size}^3, {iters} fixed iterations per step (epsil=0; the GPU arm's per-iteration "
+              f"rate is compared), iso, nonneg; warm-up steps run 1 iteration")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"FGP_TV 3D {args.size}^3 phantom", "lambda": LAM, "iterations_per_step": iters},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "config": {"workload": f"FGP_TV 3D {args.size}^3 ellipsoid phantom + noise", "lambda": LAM,
+                   "methodTV": "iso", "nonneg": NONNEG, "iterations_per_step": iters},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                         **host_info()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -313,45 +337,138 @@ def batch_volumes(n=64, seed=2):
     return [noisy_phantom(tuple(int(e) for e in sh), 30, 1000 + i) for i, sh in enumerate(shapes)]
 
 
+def reference_gpu_lib():
+    """The reference's own CUDA library (its *_GPU_main per-call path, compiled
+    for sm_103a from the staged reference sources into oracle/_ref), or None
+    when the sources are not staged on this machine."""
+    import ctypes
+
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "refgpu"], capture_output=True, text=True)
+    path = os.path.join(ROOT, "oracle", "_ref", "libcilregcuda_ref.so")
+    if r.returncode != 0 or not os.path.exists(path):
+        return None
+    lib = ctypes.CDLL(path)
+    P, F, I = ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_int
+    # TV_FGP_GPU_core.h:7, TGV_GPU_core.h:8, TV_ROF_GPU_core.h:6, TV_SB_GPU_core.h:8, NonlDiff_GPU_core.h:6
+    lib.TV_FGP_GPU_main.argtypes = [P, P, P, F, I, F, I, I, I, I, I, I]
+    lib.TGV_GPU_main.argtypes = [P, P, P, F, F, F, I, F, F, I, I, I, I]
+    lib.TV_ROF_GPU_main.argtypes = [P, P, P, F, I, F, F, I, I, I, I]
+    lib.TV_SB_GPU_main.argtypes = [P, P, P, F, I, F, I, I, I, I, I]
+    lib.NonlDiff_GPU_main.argtypes = [P, P, P, F, F, I, F, I, F, I, I, I, I]
+    for name in ("TV_FGP_GPU_main", "TGV_GPU_main", "TV_ROF_GPU_main", "TV_SB_GPU_main", "NonlDiff_GPU_main"):
+        getattr(lib, name).restype = ctypes.c_int
+    return lib
+
+
+def reference_tgv_in_bounds(shape):
+    """The reference's 3D TGV kernels index element (i, j, k) as
+    (dimX*dimY)*k + i*dimX + j (TGV_GPU_core.cu:290) while TV.py:722-731 passes
+    the array shape (Z, Y, X) as (dimX, dimY, dimZ); every index stays inside
+    the array only when Z <= Y.  Other shapes would read and write past the
+    end of the last plane, so the baseline never runs them."""
+    return len(shape) == 3 and shape[0] <= shape[1]
+
+
+def _ref_call(lib, name, vol, *args):
+    """One per-call reference GPU run from host arrays, its dims as TV.py passes them."""
+    import ctypes
+
+    P = ctypes.POINTER(ctypes.c_float)
+    a = np.ascontiguousarray(vol, dtype=np.float32)
+    out = np.zeros_like(a)
+    info = np.zeros(2, np.float32)
+    if name == "TGV_GPU_main":
+        dims = list(a.shape)  # TV.py:722-725 reverses the dims twice: (Z, Y, X)
+    else:
+        dims = list(a.shape)[::-1] + ([1] if a.ndim == 2 else [])
+    st = getattr(lib, name)(a.ctypes.data_as(P), out.ctypes.data_as(P), info.ctypes.data_as(P), *args, 0, *dims)
+    if st != 0:
+        raise RuntimeError(f"reference {name} returned {st}")
+    return out
+
+
 def batch_bench(args):
     """Batched FGP-TV and TGV (one graph launch per regulariser) against the
-    same volumes regularised one call at a time through the device API."""
+    same volumes regularised one call at a time: through this library's device
+    API, and through the reference's own per-call GPU path (TV_FGP_GPU_main,
+    TGV_GPU_main with host arrays, as TV.py calls them).  The batched run is
+    timed both on device-resident volumes and from host arrays (copies in and
+    out included), the latter being the like-for-like comparison with the
+    reference's host-array calls."""
     import torch
     from ccpi.filters import regularisersCuPy as D
     from ccpi.filters.batch import FGP_TV_batch, TGV_batch
 
-    vols = [torch.from_numpy(v).cuda() for v in batch_volumes()]
+    host = batch_volumes()
+    vols = [torch.from_numpy(v).cuda() for v in host]
     nvox = sum(v.numel() for v in vols)
     iters = 300
+    tgv_sub = [i for i, v in enumerate(host) if reference_tgv_in_bounds(v.shape)]
     runs = {
         "FGP_TV": (lambda: FGP_TV_batch(vols, 0.03, iters, 0.0, 0, 1),
-                   lambda: [D.FGP_TV(v, 0.03, iters, 0.0, 0, 1) for v in vols]),
+                   lambda: FGP_TV_batch(host, 0.03, iters, 0.0, 0, 1),
+                   lambda: [D.FGP_TV(v, 0.03, iters, 0.0, 0, 1) for v in vols],
+                   list(range(len(host))),
+                   lambda lib, v: _ref_call(lib, "TV_FGP_GPU_main", v, 0.03, iters, 0.0, 0, 1)),
         "TGV": (lambda: TGV_batch(vols, 0.03, 1.0, 2.0, iters, 12.0),
-                lambda: [D.TGV(v, 0.03, 1.0, 2.0, iters, 12.0) for v in vols]),
+                lambda: TGV_batch(host, 0.03, 1.0, 2.0, iters, 12.0),
+                lambda: [D.TGV(v, 0.03, 1.0, 2.0, iters, 12.0) for v in vols],
+                tgv_sub,
+                lambda lib, v: _ref_call(lib, "TGV_GPU_main", v, 0.03, 1.0, 2.0, iters, 12.0, 0.0)),
     }
 
     def timed(fn):
         torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record()
+        t = time.perf_counter()
         fn()
-        b.record()
         torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3
+        return time.perf_counter() - t
 
+    ref = reference_gpu_lib() if not args.no_reference_gpu else None
     out = {"workload": f"{len(vols)} volumes, edges from {{96,128,160,192,256}}, {nvox} voxels, {iters} iterations",
            "results": {}}
-    for name, (batched, percall) in runs.items():
+    for name, (batched, batched_host, percall, ref_idx, ref_fn) in runs.items():
         timed(batched)
         tb = min(timed(batched) for _ in range(max(1, args.steps)))
+        timed(batched_host)
+        tbh = min(timed(batched_host) for _ in range(max(1, min(args.steps, 2))))
         timed(percall)
         tp = min(timed(percall) for _ in range(max(1, min(args.steps, 2))))
-        out["results"][name] = {
-            "batched_s": tb, "per_call_s": tp, "batched_volumes_per_s": len(vols) / tb,
-            "per_call_volumes_per_s": len(vols) / tp, "batched_voxel_iters_per_s": nvox * iters / tb,
-            "speedup_vs_per_call": tp / tb}
-        print(json.dumps({name: out["results"][name]}))
+        r = {"batched_s": tb, "batched_from_host_s": tbh, "per_call_s": tp,
+             "batched_volumes_per_s": len(vols) / tb, "batched_from_host_volumes_per_s": len(vols) / tbh,
+             "per_call_volumes_per_s": len(vols) / tp, "batched_voxel_iters_per_s": nvox * iters / tb,
+             "speedup_vs_per_call": tp / tb}
+        if ref is not None:
+            sub = [host[i] for i in ref_idx]
+            sub_vox = sum(v.size for v in sub)
+            _ref_call_warm = ref_fn(ref, sub[0])  # module load, context
+            del _ref_call_warm
+            t = time.perf_counter()
+            for v in sub:
+                ref_fn(ref, v)
+            tr = time.perf_counter() - t
+            # this library on exactly the same volumes, batched from host arrays
+            sub_fn = (lambda: FGP_TV_batch(sub, 0.03, iters, 0.0, 0, 1)) if name == "FGP_TV" else \
+                (lambda: TGV_batch(sub, 0.03, 1.0, 2.0, iters, 12.0))
+            sub_dev = [vols[i] for i in ref_idx]
+            sub_dev_fn = (lambda: FGP_TV_batch(sub_dev, 0.03, iters, 0.0, 0, 1)) if name == "FGP_TV" else \
+                (lambda: TGV_batch(sub_dev, 0.03, 1.0, 2.0, iters, 12.0))
+            timed(sub_fn)
+            ts = min(timed(sub_fn) for _ in range(2))
+            timed(sub_dev_fn)
+            tsd = min(timed(sub_dev_fn) for _ in range(2))
+            r["reference_per_call"] = {
+                "volumes": len(sub), "voxels": sub_vox,
+                "selection": ("all volumes" if len(sub) == len(host) else
+                              "volumes with shape[0] <= shape[1], the only ones the reference kernels index in bounds"),
+                "reference_s": tr, "reference_volumes_per_s": len(sub) / tr,
+                "batched_from_host_s": ts, "batched_from_host_volumes_per_s": len(sub) / ts,
+                "batched_device_s": tsd, "batched_device_volumes_per_s": len(sub) / tsd,
+                "speedup_from_host": tr / ts, "speedup_device_resident": tr / tsd}
+        out["results"][name] = r
+        print(json.dumps({name: r}))
+    if ref is None:
+        out["reference_per_call"] = "unavailable: the reference sources are not staged on this machine"
     print(json.dumps(out))
     return 0
 
@@ -477,7 +594,7 @@ def configs_bench(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     use_ref = O.ref_lib() is not None
     kind, cores = ("reference" if use_ref else "port"), O.num_threads()
 
@@ -544,8 +661,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
-    ap.add_argument("--ref-iters", type=int, default=4, help="iterations per reference-arm step")
-    ap.add_argument("--cpu-iters", type=int, default=6, help="iterations of the cpu_baseline sample")
+    ap.add_argument("--ref-iters", type=int, default=20, help="iterations per reference-arm step")
+    ap.add_argument("--cpu-iters", type=int, default=20, help="iterations of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
@@ -559,6 +676,8 @@ def main():
     ap.add_argument("--serve", action="store_true",
                     help="Poisson stream (mean 200 req/s) of prox requests through the continuous-batching server")
     ap.add_argument("--requests", type=int, default=48, help="requests of the --serve stream")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="--batch / --serve: skip the reference's per-call GPU path")
     ap.add_argument("--configs", action="store_true",
                     help="configs C1 and C2 through the Python API (host arrays) beside the reference CPU")
     ap.add_argument("--regs", default="", help="comma-separated regularisers of --suite (default: all)")
@@ -664,6 +783,8 @@ def main():
     tpv = _ncu_traffic_per_voxel()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": (tpv * n if tpv is not None else None), "peak_kind": peak_kind,
+                "traffic_source": ("not measured in this run: the ncu DRAM bytes per voxel-iteration of "
+                                   "profiles/fgp_tv_3d_kernel.md scaled to this launch"),
                 "kernel": fgp_kernel_name(nx), "launch_ms": per_launch * 1e3,
                 "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_ITER * n}
 
@@ -696,7 +817,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, kind, cores, dt = cpu_baseline(x, args.cpu_iters)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
-               "sample": f"FGP_TV {args.size}^3, {args.cpu_iters} fixed iterations (epsil=0), {dt:.1f} s"}
+               "sample": f"FGP_TV {args.size}^3, {args.cpu_iters} fixed iterations (epsil=0), {dt:.1f} s",
+               **host_info()}
 
     if rank == 0:
         line = {

@@ -194,15 +194,17 @@ static void rof_update(const float *D1, const float *D2, const float *D3, float 
     }
 }
 
-float port_TV_ROF(float *Input, float *Output, float *infovector, float *lambdaPar, int lambda_is_arr,
-                  int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ)
+/* u_init (optional) replaces Input as the starting iterate: the warm start of
+ * a prox session, whose ROF and NDF proxes continue from the previous output */
+static float rof_main(float *Input, float *Output, float *infovector, float *lambdaPar, int lambda_is_arr,
+                      int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ, const float *u_init)
 {
     if (dimZ < 1) dimZ = 1; /* a missing third axis means one slice */
     idx_t nx = dimX, ny = dimY, nz = dimZ, n = nx * ny * nz;
     float *D1 = zalloc(n), *D2 = zalloc(n), *D3 = zalloc(n), *Uprev = NULL;
     stop_state st = {0.0f, 0};
     int it;
-    copy_arr(Input, Output, n);
+    copy_arr(u_init ? u_init : Input, Output, n);
     if (epsil != 0.0f) Uprev = zalloc(n);
     for (it = 0; it < iterationsNumb; it++) {
         int check = (epsil != 0.0f) && (it % 5 == 0);
@@ -215,6 +217,20 @@ float port_TV_ROF(float *Input, float *Output, float *infovector, float *lambdaP
     infovector[0] = (float)it;
     infovector[1] = st.re;
     return 0;
+}
+
+float port_TV_ROF(float *Input, float *Output, float *infovector, float *lambdaPar, int lambda_is_arr,
+                  int iterationsNumb, float tau, float epsil, int dimX, int dimY, int dimZ)
+{
+    return rof_main(Input, Output, infovector, lambdaPar, lambda_is_arr, iterationsNumb, tau, epsil, dimX, dimY,
+                    dimZ, NULL);
+}
+
+float port_TV_ROF_init(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
+                       float tau, float epsil, int dimX, int dimY, int dimZ, const float *u_init)
+{
+    return rof_main(Input, Output, infovector, &lambdaPar, 0, iterationsNumb, tau, epsil, dimX, dimY, dimZ,
+                    u_init);
 }
 
 /* ------------------------------------------------------------------ */
@@ -260,8 +276,12 @@ static void clamp_nonneg(float *U, idx_t n)
 /* ------------------------------------------------------------------ */
 /* FGP-TV  (FGP_TV_core.c:40-269)                                      */
 /* ------------------------------------------------------------------ */
-float port_TV_FGP(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
-                  float epsil, int methodTV, int nonneg, int dimX, int dimY, int dimZ)
+/* pstate (optional, na arrays of n floats back to back): the dual iterate a
+ * previous call ended with.  R and P_prev start from it instead of zero (the
+ * momentum restarts at t = 1, so the first R is exactly that P), and the last
+ * P is written back to it: the warm start of a prox session. */
+static float fgp_main(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
+                      float epsil, int methodTV, int nonneg, int dimX, int dimY, int dimZ, float *pstate)
 {
     if (dimZ < 1) dimZ = 1; /* a missing third axis means one slice */
     int three = dimZ > 1;
@@ -272,6 +292,8 @@ float port_TV_FGP(float *Input, float *Output, float *infovector, float lambdaPa
     float multip = three ? (1.0f / (12.0f * lambdaPar)) : (1.0f / (8.0f * lambdaPar));
     stop_state st = {0.0f, 0};
     for (c = 0; c < na; c++) { P[c] = zalloc(n); Pold[c] = zalloc(n); R[c] = zalloc(n); }
+    if (pstate)
+        for (c = 0; c < na; c++) { copy_arr(pstate + c * n, R[c], n); copy_arr(pstate + c * n, Pold[c], n); }
     if (epsil != 0.0f) Uprev = zalloc(n);
 
     for (it = 0; it < iterationsNumb; it++) {
@@ -328,11 +350,27 @@ float port_TV_FGP(float *Input, float *Output, float *infovector, float lambdaPa
             if (check && stop_check(&st, Output, Uprev, n, epsil)) break;
         }
     }
+    if (pstate)
+        for (c = 0; c < na; c++) copy_arr(P[c], pstate + c * n, n);
     for (c = 0; c < na; c++) { free(P[c]); free(Pold[c]); free(R[c]); }
     free(Uprev);
     infovector[0] = (float)it;
     infovector[1] = st.re;
     return 0;
+}
+
+float port_TV_FGP(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
+                  float epsil, int methodTV, int nonneg, int dimX, int dimY, int dimZ)
+{
+    return fgp_main(Input, Output, infovector, lambdaPar, iterationsNumb, epsil, methodTV, nonneg, dimX, dimY, dimZ,
+                    NULL);
+}
+
+float port_TV_FGP_warm(float *Input, float *Output, float *infovector, float lambdaPar, int iterationsNumb,
+                       float epsil, int methodTV, int nonneg, int dimX, int dimY, int dimZ, float *pstate)
+{
+    return fgp_main(Input, Output, infovector, lambdaPar, iterationsNumb, epsil, methodTV, nonneg, dimX, dimY, dimZ,
+                    pstate);
 }
 
 /* ------------------------------------------------------------------ */
@@ -467,8 +505,11 @@ static void sb_shrink_bregman(const float *U, float *const *D, float *const *B, 
             }
 }
 
-float port_SB_TV(float *Input, float *Output, float *infovector, float mu, int iter, float epsil, int methodTV,
-                 int dimX, int dimY, int dimZ)
+/* dbstate (optional, 2*na arrays of n floats: D components then B
+ * components): the split and Bregman variables a previous call ended with;
+ * they replace the zero start and receive the final D, B. */
+static float sb_main(float *Input, float *Output, float *infovector, float mu, int iter, float epsil, int methodTV,
+                     int dimX, int dimY, int dimZ, float *dbstate)
 {
     if (dimZ < 1) dimZ = 1; /* a missing third axis means one slice */
     int three = dimZ != 1;
@@ -480,6 +521,8 @@ float port_SB_TV(float *Input, float *Output, float *infovector, float mu, int i
     mu = 1.0f / mu;
     lambda = 2.0f * mu;
     for (c = 0; c < na; c++) { D[c] = zalloc(n); B[c] = zalloc(n); }
+    if (dbstate)
+        for (c = 0; c < na; c++) { copy_arr(dbstate + c * n, D[c], n); copy_arr(dbstate + (na + c) * n, B[c], n); }
     copy_arr(Input, Output, n);
     for (it = 0; it < iter; it++) {
         copy_arr(Output, Uprev, n);
@@ -489,11 +532,25 @@ float port_SB_TV(float *Input, float *Output, float *infovector, float mu, int i
         sb_shrink_bregman(Output, D, B, three, methodTV == 1, nx, ny, nz, lambda);
         if ((epsil != 0.0f) && (it % 5 == 0) && stop_check(&st, Output, Uprev, n, epsil)) break;
     }
+    if (dbstate)
+        for (c = 0; c < na; c++) { copy_arr(D[c], dbstate + c * n, n); copy_arr(B[c], dbstate + (na + c) * n, n); }
     for (c = 0; c < na; c++) { free(D[c]); free(B[c]); }
     free(Uprev);
     infovector[0] = (float)it;
     infovector[1] = st.re;
     return 0;
+}
+
+float port_SB_TV(float *Input, float *Output, float *infovector, float mu, int iter, float epsil, int methodTV,
+                 int dimX, int dimY, int dimZ)
+{
+    return sb_main(Input, Output, infovector, mu, iter, epsil, methodTV, dimX, dimY, dimZ, NULL);
+}
+
+float port_SB_TV_warm(float *Input, float *Output, float *infovector, float mu, int iter, float epsil,
+                      int methodTV, int dimX, int dimY, int dimZ, float *dbstate)
+{
+    return sb_main(Input, Output, infovector, mu, iter, epsil, methodTV, dimX, dimY, dimZ, dbstate);
 }
 
 /* ------------------------------------------------------------------ */
@@ -686,9 +743,9 @@ static void ndf_sweep(const float *F, const float *Src, float *Dst, float lambda
             }
 }
 
-float port_Diffusion(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
-                     int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ,
-                     int jacobi)
+static float ndf_main(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                      int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ,
+                      int jacobi, const float *u_init)
 {
     if (dimZ < 1) dimZ = 1; /* a missing third axis means one slice */
     int three = dimZ != 1;
@@ -702,7 +759,7 @@ float port_Diffusion(float *Input, float *Output, float *infovector, float lambd
         return -1.0f;
     }
     if (epsil != 0.0f) Uprev = zalloc(n);
-    copy_arr(Input, Output, n);
+    copy_arr(u_init ? u_init : Input, Output, n);
     for (it = 0; it < iterationsNumb; it++) {
         int check = (epsil != 0.0f) && (it % 5 == 0);
         if (check) copy_arr(Output, Uprev, n);
@@ -718,6 +775,22 @@ float port_Diffusion(float *Input, float *Output, float *infovector, float lambd
     infovector[0] = (float)it;
     infovector[1] = st.re;
     return 0;
+}
+
+float port_Diffusion(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                     int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ,
+                     int jacobi)
+{
+    return ndf_main(Input, Output, infovector, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype, epsil, dimX,
+                    dimY, dimZ, jacobi, NULL);
+}
+
+float port_Diffusion_init(float *Input, float *Output, float *infovector, float lambdaPar, float sigmaPar,
+                          int iterationsNumb, float tau, int penaltytype, float epsil, int dimX, int dimY, int dimZ,
+                          const float *u_init)
+{
+    return ndf_main(Input, Output, infovector, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype, epsil, dimX,
+                    dimY, dimZ, 1, u_init);
 }
 
 /* ------------------------------------------------------------------ */

@@ -58,6 +58,12 @@ def port_lib():
             raise RuntimeError(f"cannot load oracle port {PORT_PATH}")
         _declare(_port, prefix="port_")
         _port.port_num_threads.restype = ctypes.c_int
+        _port.port_TV_ROF_init.argtypes = [_P, _P, _P, _F, _I, _F, _F, _I, _I, _I, _P]
+        _port.port_TV_FGP_warm.argtypes = [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I, _I, _P]
+        _port.port_SB_TV_warm.argtypes = [_P, _P, _P, _F, _I, _F, _I, _I, _I, _I, _P]
+        _port.port_Diffusion_init.argtypes = [_P, _P, _P, _F, _F, _I, _F, _I, _F, _I, _I, _I, _P]
+        for name in ("port_TV_ROF_init", "port_TV_FGP_warm", "port_SB_TV_warm", "port_Diffusion_init"):
+            getattr(_port, name).restype = ctypes.c_float
         _port.port_set_trace.argtypes = [_P, ctypes.c_int]
         _port.port_trace_len.restype = ctypes.c_int
     return _port
@@ -235,6 +241,64 @@ def tv_energy(u, u0, lam, typ, use_ref=False):
         fn = lib.port_TV_energy3D if is_port else lib.TV_energy3D
         fn(_ptr(u), _ptr(u0), _ptr(e), lam, typ, u.shape[2], u.shape[1], u.shape[0])
     return float(e[0])
+
+
+class WarmProx:
+    """A regulariser whose state persists across calls, as in a prox session
+    of the library: FGP keeps its last dual iterate P (the next call's R and
+    P_prev start from it), SB its split and Bregman variables D, B, ROF and
+    NDF (Jacobi order) start from the previous output.  The first call is
+    the plain cold call.  `alg` is 0 ROF (lambda, tau), 1 FGP (lambda,
+    methodTV, nonneg), 2 SB (mu, methodTV), 3 NDF (lambda, sigma, tau,
+    penalty)."""
+
+    def __init__(self, alg, params, shape):
+        self.alg, self.prm = int(alg), [float(p) for p in params]
+        self.shape = tuple(shape)
+        n = int(np.prod(self.shape))
+        na = 3 if len(self.shape) == 3 and self.shape[0] > 1 else 2
+        self.state = np.zeros(n * (na if alg == 1 else 2 * na if alg == 2 else 0), np.float32)
+        self.prev = None
+
+    def __call__(self, z, iters):
+        lib = port_lib()
+        a, out, info = _prep(z)
+        d = _dims(a)
+        p = self.prm
+        u0 = _ptr(self.prev) if self.prev is not None else None
+        if self.alg == 0:
+            lib.port_TV_ROF_init(_ptr(a), _ptr(out), _ptr(info), p[0], iters, p[1], 0.0, *d, u0)
+        elif self.alg == 1:
+            lib.port_TV_FGP_warm(_ptr(a), _ptr(out), _ptr(info), p[0], iters, 0.0, int(p[1]), int(p[2]), *d,
+                                 _ptr(self.state))
+        elif self.alg == 2:
+            lib.port_SB_TV_warm(_ptr(a), _ptr(out), _ptr(info), p[0], iters, 0.0, int(p[1]), *d,
+                                _ptr(self.state))
+        else:
+            lib.port_Diffusion_init(_ptr(a), _ptr(out), _ptr(info), p[0], p[1], iters, p[2], int(p[3]), 0.0, *d,
+                                    u0)
+        if self.alg in (0, 3):
+            self.prev = out.copy()
+        return out
+
+
+def fista(alg, f, params, outer, inner, step):
+    """FISTA on min_x 1/2 ||x - f||^2 + R(x) with warm-started proxes, in FP32
+    as the library's session loop: z = y - step (y - f); x+ = prox(z) (inner
+    iterations, warm state kept); t+ = (1 + sqrt(1 + 4 t^2)) / 2;
+    y = x+ + ((t - 1) / t+)(x+ - x).  Starts from x = y = f, t = 1."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    prox = WarmProx(alg, params, f.shape)
+    x, y, t = f.copy(), f.copy(), np.float32(1.0)
+    st = np.float32(step)
+    for _ in range(outer):
+        z = (y - st * (y - f)).astype(np.float32)
+        xn = prox(z, inner)
+        tn = np.float32((np.float32(1.0) + np.sqrt(np.float32(1.0) + np.float32(4.0) * t * t)) * np.float32(0.5))
+        beta = np.float32((t - np.float32(1.0)) / tn)
+        y = (xn + beta * (xn - x)).astype(np.float32)
+        x, t = xn, tn
+    return x
 
 
 def num_threads() -> int:
