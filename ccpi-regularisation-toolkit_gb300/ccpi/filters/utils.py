@@ -3,7 +3,9 @@ src/Python/ccpi/filters/utils.py:13-23 loads ``libcilreg`` and
 ``libcilregcuda`` from this directory the same way).
 
 Both libraries are required: there is no CPU fallback.  If they are missing,
-build them with ``python build.py`` in the package root.
+build them with ``python build.py`` in the package root.  ``libcilreg.so``
+forwards every entry point to ``libcilregcuda.so``, so the process holds one
+copy of the GPU library whichever name a caller binds.
 """
 import ctypes
 import os
@@ -79,7 +81,11 @@ _SESSION_SIGS = {
     "cilreg_prox_session_create": [ctypes.POINTER(ctypes.c_void_p), _I, _P, _I, _I, _I, _I, _V],
     "cilreg_prox_session_prox": [_V, _V, _V, _I, _F, _P, _V],
     "cilreg_prox_session_fista": [_V, _V, _V, _I, _I, _F, _V],
+    "cilreg_prox_session_admm": [_V, _V, _V, _V, _I, _I, _F, _V],
+    "cilreg_prox_session_pdhg": [_V, _V, _V, _V, _I, _I, _F, _F, _V],
+    "cilreg_prox_session_set_cancel": [_V, _IP],
     "cilreg_prox_session_destroy": [_V, _V],
+    "cilreg_debug_fail_allocations": [_I],
 }
 _BATCH_SIGS = {
     "cilreg_fgp_tv_batch_dev": [_I, _PP, _PP, _IP, _P, _I, _F, _I, _I, _P, _V],
@@ -104,7 +110,8 @@ for _lib in (cilreg, cilregcuda):
 
 
 class RegulariserError(RuntimeError):
-    """A regulariser call returned a failure status."""
+    """A regulariser call returned a failure status (-1 CUDA, -3 no device,
+    -4 out of memory, -5 cancelled)."""
 
     def __init__(self, status: int, message: str):
         super().__init__(f"status {status}: {message}")
@@ -131,16 +138,15 @@ def device_count() -> int:
 
 
 def launch_count() -> int:
-    """Kernels launched so far by the library (both names share one counter only
-    when loaded as one object; each loaded library counts its own launches)."""
-    return int(cilregcuda.cilreg_launch_count()) + int(cilreg.cilreg_launch_count())
+    """Kernels launched so far by the library in this process (libcilreg.so
+    forwards to libcilregcuda.so, so both names share one counter)."""
+    return int(cilregcuda.cilreg_launch_count())
 
 
 def release_cached(gpu_device: int = 0) -> None:
     """Wait for the device's work and hand back the scratch memory the library
     keeps cached in the device's stream-ordered pool."""
-    for lib in (cilregcuda, cilreg):
-        check_status(lib.cilreg_release_cached(int(gpu_device)), lib)
+    check_status(cilregcuda.cilreg_release_cached(int(gpu_device)))
 
 
 def loaded_libraries():

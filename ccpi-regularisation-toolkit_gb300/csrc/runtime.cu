@@ -129,9 +129,26 @@ Scratch::~Scratch() {
         if (ptrs_[i]) cudaFreeAsync(ptrs_[i], stream_);
 }
 
+namespace {
+std::atomic<int> g_injected_failures{0};
+}
+
+void inject_allocation_failures(int n) { g_injected_failures.store(n < 0 ? 0 : n); }
+
+bool take_injected_failure() {
+    int v = g_injected_failures.load();
+    while (v > 0)
+        if (g_injected_failures.compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
+
 void* Scratch::bytes(size_t n) {
     if (n_ >= kMax) {
         status_ = fail(ERR_ARG, __FILE__, __LINE__, "scratch slot table exhausted");
+        return nullptr;
+    }
+    if (take_injected_failure()) {
+        status_ = fail(ERR_OOM, __FILE__, __LINE__, "scratch allocation of %zu bytes failed: injected failure", n);
         return nullptr;
     }
     void* p = nullptr;

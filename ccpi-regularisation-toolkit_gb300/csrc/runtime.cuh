@@ -21,7 +21,14 @@ enum Status : int {
     ERR_ARG = -2,
     ERR_NODEV = -3,
     ERR_OOM = -4,
+    ERR_CANCELLED = -5,
 };
+
+// Host-side fault injection for tests: the next `n` device allocations the
+// library makes (scratch and prox sessions) fail as if the device were full.
+void inject_allocation_failures(int n);
+// true (and one fewer pending failure) when an injected failure is due
+bool take_injected_failure();
 
 // record an error (thread-local message, also printed to stderr like the
 // reference's CHECK macro) and return the status

@@ -56,6 +56,58 @@ __global__ void k_momentum(float* __restrict__ y, const float* __restrict__ xn, 
     for (; i < n; i += stride) y[i] = xn[i] + beta * (xn[i] - x[i]);
 }
 
+// ADMM (scaled form) on min_x 1/2 ||w^(1/2)(x - f)||^2 + R(x) with the
+// splitting x = z:  x = (w f + rho (z - u)) / (w + rho),  v = x + u  (the
+// prox argument; z = prox(v) follows),  then  u = u + x - z.
+__global__ void k_admm_xv(float* __restrict__ x, float* __restrict__ v, const float* __restrict__ z,
+                          const float* __restrict__ u, const float* __restrict__ f, const float* __restrict__ w,
+                          float rho, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) {
+        const float wi = w ? w[i] : 1.0f;
+        const float xi = __fdiv_rn(__fadd_rn(__fmul_rn(wi, f[i]), __fmul_rn(rho, __fsub_rn(z[i], u[i]))),
+                                   __fadd_rn(wi, rho));
+        x[i] = xi;
+        v[i] = __fadd_rn(xi, u[i]);
+    }
+}
+
+__global__ void k_admm_u(float* __restrict__ u, const float* __restrict__ x, const float* __restrict__ z,
+                         long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) u[i] = __fsub_rn(__fadd_rn(u[i], x[i]), z[i]);
+}
+
+// PDHG (Chambolle-Pock, K = I) on the same problem with the regulariser as
+// the dual term:  y+ = prox_{sigma R*}(y + sigma xbar) = sigma (q - prox_{R/sigma}(q))
+// with q = y / sigma + xbar;  x+ = (x - tau y+ + tau w f) / (1 + tau w);
+// xbar = 2 x+ - x.  q is formed in place over xbar.
+__global__ void k_pdhg_q(float* __restrict__ q, const float* __restrict__ y, float inv_sigma, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) q[i] = __fadd_rn(__fmul_rn(y[i], inv_sigma), q[i]);
+}
+
+__global__ void k_pdhg_primal(float* __restrict__ x, float* __restrict__ y, float* __restrict__ qbar,
+                              const float* __restrict__ p, const float* __restrict__ f, const float* __restrict__ w,
+                              float tau, float sigma, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) {
+        const float wi = w ? w[i] : 1.0f;
+        const float yi = __fmul_rn(sigma, __fsub_rn(qbar[i], p[i]));
+        const float tw = __fmul_rn(tau, wi);
+        const float xo = x[i];
+        const float xn = __fdiv_rn(__fadd_rn(__fsub_rn(xo, __fmul_rn(tau, yi)), __fmul_rn(tw, f[i])),
+                                   __fadd_rn(1.0f, tw));
+        y[i] = yi;
+        x[i] = xn;
+        qbar[i] = __fsub_rn(__fmul_rn(2.0f, xn), xo);
+    }
+}
+
 dim3 ew_grid(long long n) {
     long long b = (n + 255) / 256;
     if (b > 152LL * 8) b = 152LL * 8;
@@ -77,6 +129,7 @@ struct cilreg_session {
     bool has_prev;
     FgpWarm fgp;
     SbWarm sb;
+    const volatile int* cancel;  // host flag: nonzero ends an outer loop after its current step
 };
 
 namespace {
@@ -111,6 +164,15 @@ int session_prox(cilreg_session* S, const float* in, float* out, int iters, floa
     return OK;
 }
 
+// between two outer steps: with a cancel flag registered, wait for the step
+// (so that cancelling takes effect within one step) and report a raised flag
+int outer_boundary(cilreg_session* S, cudaStream_t s) {
+    if (!S->cancel) return OK;
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    if (*S->cancel) return fail(ERR_CANCELLED, __FILE__, __LINE__, "cancelled");
+    return OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -132,6 +194,11 @@ int cilreg_prox_session_create(cilreg_session** out, int alg, const float* param
         return fail(ERR_ARG, __FILE__, __LINE__, "algorithm %d needs %d parameters", alg, need[alg]);
     cilreg_session* S = new (std::nothrow) cilreg_session();
     if (!S) return fail(ERR_OOM, __FILE__, __LINE__, "host allocation failed");
+    S->cancel = nullptr;
+    if (take_injected_failure()) {
+        delete S;
+        return fail(ERR_OOM, __FILE__, __LINE__, "session allocation failed: injected failure");
+    }
     S->alg = alg;
     S->d = make_dims(dimX, dimY, dimZ < 1 ? 1 : dimZ);
     for (int i = 0; i < 4; i++) S->prm[i] = (i < nparams) ? params[i] : 0.0f;
@@ -202,6 +269,7 @@ int cilreg_prox_session_fista(cilreg_session* S, const float* d_f, float* d_x, i
     CILREG_CUDA(cudaMemcpyAsync(S->y, d_f, nb, cudaMemcpyDeviceToDevice, s));
     float t = 1.0f;
     for (int k = 0; k < outer; k++) {
+        CILREG_TRY(outer_boundary(S, s));
         k_grad_step<<<ew_grid(n), 256, 0, s>>>(S->z, S->y, d_f, step, n);  // gradient of 1/2 ||y - f||^2
         CILREG_CUDA(cudaGetLastError());
         note_launch();
@@ -217,6 +285,71 @@ int cilreg_prox_session_fista(cilreg_session* S, const float* d_f, float* d_x, i
     }
     CILREG_CUDA(cudaMemcpyAsync(d_x, S->x, nb, cudaMemcpyDeviceToDevice, s));
     CILREG_CUDA(cudaStreamSynchronize(s));
+    return OK;
+}
+
+int cilreg_prox_session_admm(cilreg_session* S, const float* d_f, const float* d_w, float* d_x, int outer, int inner,
+                             float rho, void* stream) {
+    if (!S || !d_f || !d_x) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
+    if (outer < 0 || inner < 0) return fail(ERR_ARG, __FILE__, __LINE__, "negative iteration count");
+    if (!(rho > 0.0f)) return fail(ERR_ARG, __FILE__, __LINE__, "rho must be positive");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = S->d.n;
+    const size_t nb = sizeof(float) * (size_t)n;
+    // x in S->x, u in S->y, the prox argument v in S->z, z in S->xn
+    CILREG_CUDA(cudaMemcpyAsync(S->xn, d_f, nb, cudaMemcpyDeviceToDevice, s));  // z = f
+    CILREG_CUDA(cudaMemsetAsync(S->y, 0, nb, s));                                  // u = 0
+    for (int k = 0; k < outer; k++) {
+        CILREG_TRY(outer_boundary(S, s));
+        k_admm_xv<<<ew_grid(n), 256, 0, s>>>(S->x, S->z, S->xn, S->y, d_f, d_w, rho, n);
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+        CILREG_TRY(session_prox(S, S->z, S->xn, inner, 0.0f, nullptr, s));
+        k_admm_u<<<ew_grid(n), 256, 0, s>>>(S->y, S->x, S->xn, n);
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+    }
+    CILREG_CUDA(cudaMemcpyAsync(d_x, S->xn, nb, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    return OK;
+}
+
+int cilreg_prox_session_pdhg(cilreg_session* S, const float* d_f, const float* d_w, float* d_x, int outer, int inner,
+                             float tau, float sigma, void* stream) {
+    if (!S || !d_f || !d_x) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
+    if (outer < 0 || inner < 0) return fail(ERR_ARG, __FILE__, __LINE__, "negative iteration count");
+    if (!(tau > 0.0f) || !(sigma > 0.0f)) return fail(ERR_ARG, __FILE__, __LINE__, "tau and sigma must be positive");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = S->d.n;
+    const size_t nb = sizeof(float) * (size_t)n;
+    // x in S->x, the dual y in S->y, xbar (then q in place) in S->z, prox(q) in S->xn
+    CILREG_CUDA(cudaMemcpyAsync(S->x, d_f, nb, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(S->z, d_f, nb, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaMemsetAsync(S->y, 0, nb, s));
+    const float inv_sigma = 1.0f / sigma;
+    for (int k = 0; k < outer; k++) {
+        CILREG_TRY(outer_boundary(S, s));
+        k_pdhg_q<<<ew_grid(n), 256, 0, s>>>(S->z, S->y, inv_sigma, n);
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+        CILREG_TRY(session_prox(S, S->z, S->xn, inner, 0.0f, nullptr, s));
+        k_pdhg_primal<<<ew_grid(n), 256, 0, s>>>(S->x, S->y, S->z, S->xn, d_f, d_w, tau, sigma, n);
+        CILREG_CUDA(cudaGetLastError());
+        note_launch();
+    }
+    CILREG_CUDA(cudaMemcpyAsync(d_x, S->x, nb, cudaMemcpyDeviceToDevice, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    return OK;
+}
+
+int cilreg_prox_session_set_cancel(cilreg_session* S, const volatile int* flag) {
+    if (!S) return fail(ERR_ARG, __FILE__, __LINE__, "null session");
+    S->cancel = flag;
+    return OK;
+}
+
+int cilreg_debug_fail_allocations(int n) {
+    inject_allocation_failures(n);
     return OK;
 }
 

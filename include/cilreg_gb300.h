@@ -229,7 +229,33 @@ int cilreg_prox_session_prox(cilreg_session *session, const float *d_in, float *
                              float *infovector, void *stream);
 int cilreg_prox_session_fista(cilreg_session *session, const float *d_f, float *d_x, int outer, int inner, float step,
                               void *stream);
+/* ADMM (scaled form) on min_x 1/2 ||w^(1/2) (x - f)||^2 + rho R(x), the
+ * session's regulariser being the prox of R (so that its parameters already
+ * carry the 1/rho): z = f, u = 0; per outer step x = (w f + rho (z - u)) /
+ * (w + rho), z = prox(x + u) (`inner` warm-started iterations), u += x - z;
+ * writes z to d_x.  d_w holds per-voxel data weights (a mask for inpainting)
+ * or is NULL for w = 1.  The splitting of the reference's reconstruction demo
+ * (demos/SoftwareX_supp/Demo_SimulData_Recon_SX.py:155-172) with the forward
+ * operator a diagonal. */
+int cilreg_prox_session_admm(cilreg_session *session, const float *d_f, const float *d_w, float *d_x, int outer,
+                             int inner, float rho, void *stream);
+/* PDHG (Chambolle-Pock with K = I) on min_x 1/2 ||w^(1/2) (x - f)||^2 +
+ * sigma R(x), the session's regulariser being the prox of R: x = xbar = f,
+ * y = 0; per outer step q = y / sigma + xbar, y = sigma (q - prox(q)),
+ * x+ = (x - tau y + tau w f) / (1 + tau w), xbar = 2 x+ - x; writes x to d_x.
+ * Convergent for tau sigma <= 1. */
+int cilreg_prox_session_pdhg(cilreg_session *session, const float *d_f, const float *d_w, float *d_x, int outer,
+                             int inner, float tau, float sigma, void *stream);
+/* Register a host flag (or NULL to remove it) that the outer loops above read
+ * before each outer step; while one is registered every outer step is waited
+ * for, and a nonzero flag ends the loop with -5 (cancelled). */
+int cilreg_prox_session_set_cancel(cilreg_session *session, const volatile int *flag);
 int cilreg_prox_session_destroy(cilreg_session *session, void *stream);
+
+/* Host-side fault injection for tests (no counterpart in the reference): the
+ * next n device allocations the library makes (scratch and prox sessions)
+ * fail with -4 as if the device were full; 0 clears it. */
+int cilreg_debug_fail_allocations(int n);
 
 /* No counterpart in the reference.  ROF-TV like cilreg_rof_tv_dev, but the
  * call allocates no device memory at all, for callers that cannot allocate

@@ -301,6 +301,47 @@ def fista(alg, f, params, outer, inner, step):
     return x
 
 
+def admm(alg, f, params, outer, inner, rho, w=None):
+    """ADMM (scaled form) on min_x 1/2 ||w^(1/2)(x - f)||^2 + rho R(x) with
+    warm-started proxes of R, in FP32 as the library's session loop (each
+    elementwise operation rounded separately): z = f, u = 0; per step
+    x = (w f + rho (z - u)) / (w + rho), z = prox(x + u), u = (u + x) - z."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    ww = np.ones_like(f) if w is None else np.ascontiguousarray(w, dtype=np.float32)
+    prox = WarmProx(alg, params, f.shape)
+    r = np.float32(rho)
+    z, u = f.copy(), np.zeros_like(f)
+    for _ in range(outer):
+        x = ((ww * f) + (r * (z - u))) / (ww + r)
+        v = x + u
+        z = prox(v.astype(np.float32), inner)
+        u = (u + x) - z
+    return z
+
+
+def pdhg(alg, f, params, outer, inner, tau, sigma, w=None):
+    """PDHG (K = I) on min_x 1/2 ||w^(1/2)(x - f)||^2 + sigma R(x) with
+    warm-started proxes of R, in FP32 as the library's session loop:
+    x = xbar = f, y = 0; per step q = y * (1/sigma) + xbar,
+    y = sigma (q - prox(q)), x+ = ((x - tau y) + (tau w) f) / (1 + tau w),
+    xbar = 2 x+ - x."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    ww = np.ones_like(f) if w is None else np.ascontiguousarray(w, dtype=np.float32)
+    prox = WarmProx(alg, params, f.shape)
+    t, sg = np.float32(tau), np.float32(sigma)
+    inv_s = np.float32(1.0) / sg
+    x, xbar, y = f.copy(), f.copy(), np.zeros_like(f)
+    for _ in range(outer):
+        q = (y * inv_s + xbar).astype(np.float32)
+        p = prox(q, inner)
+        y = sg * (q - p)
+        tw = t * ww
+        xn = ((x - t * y) + tw * f) / (np.float32(1.0) + tw)
+        xbar = np.float32(2.0) * xn - x
+        x = xn
+    return x
+
+
 def num_threads() -> int:
     return int(port_lib().port_num_threads())
 

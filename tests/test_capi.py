@@ -39,6 +39,21 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
+def test_both_library_names_share_one_copy():
+    """libcilreg.so forwards to libcilregcuda.so: an error recorded through one
+    name is the one the other reports, and both count the same launches."""
+    cpu = ctypes.CDLL(os.path.join(PKG, "ccpi", "filters", "libcilreg.so"))
+    gpu = ctypes.CDLL(os.path.join(PKG, "ccpi", "filters", "libcilregcuda.so"))
+    cpu.cilreg_prox_session_create.restype = ctypes.c_int
+    assert cpu.cilreg_prox_session_create(None, 0, None, 0, 1, 1, 1, None) == -2
+    gpu.cilreg_last_error.restype = ctypes.c_char_p
+    assert b"null session pointer" in gpu.cilreg_last_error()
+    cpu.cilreg_launch_count.restype = gpu.cilreg_launch_count.restype = ctypes.c_longlong
+    assert cpu.cilreg_launch_count() == gpu.cilreg_launch_count()
+    maps = open("/proc/self/maps").read()
+    assert len({ln.split()[-1] for ln in maps.splitlines() if ln.endswith("libcilregcuda.so")}) == 1
+
+
 def test_python_signatures_match_reference():
     from ccpi.filters import TV, diffusion, regularisersCuPy
 
