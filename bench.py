@@ -564,7 +564,35 @@ def serve_requests(n, seed=3, rate=200.0):
     return reqs
 
 
+def reference_fista(lib, req):
+    """The plain per-call GPU path for one served request: FISTA on the host
+    (numpy) around the reference's *_GPU_main called with host arrays for
+    every prox (its state discarded after each call, TV_FGP_GPU_core.cu:586-598)."""
+    f = np.ascontiguousarray(req.volume, dtype=np.float32)
+    x, y, t = f.copy(), f.copy(), np.float32(1.0)
+    st = np.float32(req.step)
+    p = req.params
+    for _ in range(req.outer):
+        z = (y - st * (y - f)).astype(np.float32)
+        if req.alg == "ROF":
+            xn = _ref_call(lib, "TV_ROF_GPU_main", z, p[0], req.inner, p[1], 0.0)
+        elif req.alg == "FGP":
+            xn = _ref_call(lib, "TV_FGP_GPU_main", z, p[0], req.inner, 0.0, int(p[1]), int(p[2]))
+        elif req.alg == "SB":
+            xn = _ref_call(lib, "TV_SB_GPU_main", z, p[0], req.inner, 0.0, int(p[1]))
+        else:
+            xn = _ref_call(lib, "NonlDiff_GPU_main", z, p[0], p[1], req.inner, p[2], int(p[3]), 0.0)
+        tn = np.float32((1.0 + np.sqrt(1.0 + 4.0 * t * t)) * 0.5)
+        y = (xn + np.float32((t - 1.0) / tn) * (xn - x)).astype(np.float32)
+        x, t = xn, tn
+    return x
+
+
 def serve_bench(args):
+    """The served workload through the continuous-batching server, then the
+    first --serve-ref-requests requests both through the server (all at once)
+    and through the reference's plain per-call GPU path (one request after
+    another, FISTA on the host, a cold reference prox per outer step)."""
     from ccpi.filters.serving import ProxServer, summarise
 
     reqs = serve_requests(args.requests)
@@ -577,6 +605,26 @@ def serve_bench(args):
     out["workload"] = (f"{len(reqs)} prox requests, Poisson mean 200/s, 2D 1024^2 / 3D 128^3-384^3, "
                        "ROF/FGP/SB/NDF, 5-50 FISTA steps x 20 inner iterations, 8 slots, 150 GB budget")
     out["volumes_per_s"] = out["requests_per_s"]
+    ref = reference_gpu_lib() if not args.no_reference_gpu else None
+    if ref is not None:
+        sub = reqs[:args.serve_ref_requests]
+        reference_fista(ref, sub[0])  # module load, context
+        t = time.perf_counter()
+        for r in sub:
+            reference_fista(ref, r)
+        tr = time.perf_counter() - t
+        t = time.perf_counter()
+        mine = server.serve(sub, realtime=False)
+        tm = time.perf_counter() - t
+        assert all(m.ok for m in mine)
+        out["reference_per_call"] = {
+            "requests": len(sub), "voxel_iters": int(sum(r.volume.size * r.outer * r.inner for r in sub)),
+            "reference_s": tr, "reference_requests_per_s": len(sub) / tr,
+            "served_s": tm, "served_requests_per_s": len(sub) / tm, "speedup": tr / tm,
+            "how": "the same requests, all available at once; reference: one request after another, FISTA on the "
+                   "host around *_GPU_main with host arrays (cold prox state each outer step)"}
+    else:
+        out["reference_per_call"] = "unavailable: the reference sources are not staged on this machine"
     print(json.dumps({"serve": out}))
     return 0
 
@@ -676,6 +724,8 @@ def main():
     ap.add_argument("--serve", action="store_true",
                     help="Poisson stream (mean 200 req/s) of prox requests through the continuous-batching server")
     ap.add_argument("--requests", type=int, default=48, help="requests of the --serve stream")
+    ap.add_argument("--serve-ref-requests", type=int, default=12,
+                    help="requests of the --serve stream also run through the reference's per-call GPU path")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="--batch / --serve: skip the reference's per-call GPU path")
     ap.add_argument("--configs", action="store_true",

@@ -36,6 +36,9 @@ int rof_launch_step(const float* cur, float* nxt, const float* f, const float* l
                     const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s);
 // number of FP64 partial slots rof_launch_step writes on a check iteration
 long long rof_partial_slots(const Dims& d);
+// OK when the kernel rof_launch_step would run for `d` fits the launch grid
+// limits, else an argument error naming the shape
+int rof_check_grid(const Dims& d);
 
 // FGP_TV_core.c:40-171.  u_out's initial content is U_prev of iteration 0.
 // warm (optional): dual state carried across calls; its ring is updated

@@ -21,7 +21,8 @@ struct PdArgs {
     float* pn[3];        // P, next
     const float* f;
     float* ubrk;         // U before extrapolation, written on check iterations
-    float sigma, tau, lt, onelt, theta;
+    float sigma, tau, lt, theta;
+    DoubleDivisor onelt;  // the reference's double (1.0 + lt)
     int nonneg, aniso, check;
 };
 
@@ -32,22 +33,16 @@ __device__ __forceinline__ void dual_at(const PdArgs& a, const Dims& d, int i, i
                                         float& p3) {
     const long long v = vid(d, i, j, k);
     const float u = ldg(a.u, v);
-    p1 = ldg(a.p[0], v) + a.sigma * (ldg(a.u, vid(d, nb_hi(i, d.nx), j, k)) - u);
-    p2 = ldg(a.p[1], v) + a.sigma * (ldg(a.u, vid(d, i, nb_hi(j, d.ny), k)) - u);
+    p1 = pd_dual(ldg(a.p[0], v), a.sigma, ldg(a.u, vid(d, nb_hi(i, d.nx), j, k)), u);
+    p2 = pd_dual(ldg(a.p[1], v), a.sigma, ldg(a.u, vid(d, i, nb_hi(j, d.ny), k)), u);
     p3 = 0.0f;
-    if (THREE) p3 = ldg(a.p[2], v) + a.sigma * (ldg(a.u, vid(d, i, j, nb_hi(k, d.nz))) - u);
+    if (THREE) p3 = pd_dual(ldg(a.p[2], v), a.sigma, ldg(a.u, vid(d, i, j, nb_hi(k, d.nz))), u);
     if (!a.aniso) {
-        const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
-        if (den > 1.0f) {
-            const float sq = rsqrtf(den);  // within 2 ulp of 1/sqrtf
-            p1 *= sq;
-            p2 *= sq;
-            p3 *= sq;
-        }
+        pd_project_iso<THREE>(p1, p2, p3);
     } else {
-        p1 = p1 / fmaxf(fabsf(p1), 1.0f);
-        p2 = p2 / fmaxf(fabsf(p2), 1.0f);
-        p3 = p3 / fmaxf(fabsf(p3), 1.0f);
+        p1 = pd_project_aniso(p1);
+        p2 = pd_project_aniso(p2);
+        p3 = pd_project_aniso(p3);
     }
 }
 
@@ -78,14 +73,14 @@ __global__ void __launch_bounds__(256) k_pd_step(PdArgs a, Dims d, int kz, const
             }
             float uo = ldg(a.u, v);
             if (a.nonneg && uo < 0.0f) uo = 0.0f;  // clamp after the dual step (:120)
-            const float unew = (uo - a.tau * dv + a.lt * ldg(a.f, v)) / a.onelt;
+            const float unew = pd_primal(uo, a.tau, dv, a.lt, ldg(a.f, v), a.onelt);
             if (a.check) {
                 const float df = unew - uo;
                 pa += df * df;
                 pb += unew * unew;
                 a.ubrk[v] = unew;
             }
-            a.un[v] = unew + a.theta * (unew - uo);  // getX (:197-205)
+            a.un[v] = pd_extrapolate(unew, a.theta, uo);  // getX (:197-205)
             a.pn[0][v] = p1;
             a.pn[1][v] = p2;
             if (THREE) a.pn[2][v] = p3;
@@ -138,6 +133,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
     const float tau = lam * 0.1f;
     const float sigma = (float)(1.0 / (double)(lipschitz * tau));
     const float lt = tau / lam;
+    const DoubleDivisor onelt = make_double_divisor(1.0 + (double)lt);  // the reference divides by (1.0 + lt)
     int it = 0;
     if (stream && !ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
@@ -154,7 +150,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
             b.sigma = sigma;
             b.tau = tau;
             b.lt = lt;
-            b.inv_onelt = (float)(1.0 / (1.0 + (double)lt));  // the reference divides by (1.0 + lt)
+            b.onelt = onelt;
             b.theta = 1.0f;
             b.nonneg = (nonneg == 1);
             b.aniso = (methodTV != 0);
@@ -179,7 +175,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
         a.sigma = sigma;
         a.tau = tau;
         a.lt = lt;
-        a.onelt = (float)(1.0 + (double)lt);
+        a.onelt = onelt;
         a.theta = 1.0f;
         a.nonneg = (nonneg == 1);
         a.aniso = (methodTV != 0);
@@ -197,7 +193,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
             b.sigma = sigma;
             b.tau = tau;
             b.lt = lt;
-            b.inv_onelt = (float)(1.0 / (1.0 + (double)lt));  // the reference divides by (1.0 + lt)
+            b.onelt = onelt;
             b.theta = 1.0f;
             b.nonneg = a.nonneg;
             b.aniso = a.aniso;

@@ -16,6 +16,7 @@
 //      lt f) / (1 + lt), writes Ue' = U + theta (U - clamp(Ue)) and P'.
 // HBM traffic: read Ue, P(3), f; write Ue, P(3) -> 36 B per voxel (28 in 2D).
 #include "pd_tiled.cuh"
+#include "pd_math.cuh"
 
 namespace cilreg {
 
@@ -76,22 +77,18 @@ __global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int
         if (plane_ok && p_pt) {
             const int sk = k & 1;
             const float c = sUe[sk][ty][tx];
-            p1 = q1 + a.sigma * (sUe[sk][ty][xh] - c);
-            p2 = q2 + a.sigma * (sUe[sk][yh][tx] - c);
+            p1 = pd_dual(q1, a.sigma, sUe[sk][ty][xh], c);
+            p2 = pd_dual(q2, a.sigma, sUe[sk][yh][tx], c);
             if (THREE) {
                 const float zhi = (nz == 1) ? c : ((k + 1 >= nz) ? um2 : uj);  // mirrored (PD_TV_core.c:225)
-                p3 = q3 + a.sigma * (zhi - c);
+                p3 = pd_dual(q3, a.sigma, zhi, c);
             }
             if (!a.aniso) {
-                const float den = THREE ? (p1 * p1 + p2 * p2 + p3 * p3) : (p1 * p1 + p2 * p2);
-                const float sq = (den > 1.f) ? rsqrtf(den) : 1.f;
-                p1 *= sq;
-                p2 *= sq;
-                p3 *= sq;
+                pd_project_iso<THREE>(p1, p2, p3);
             } else {
-                p1 = p1 / fmaxf(fabsf(p1), 1.f);
-                p2 = p2 / fmaxf(fabsf(p2), 1.f);
-                p3 = p3 / fmaxf(fabsf(p3), 1.f);
+                p1 = pd_project_aniso(p1);
+                p2 = pd_project_aniso(p2);
+                p3 = pd_project_aniso(p3);
             }
             sP1[sk][ty][tx] = p1;
             sP2[sk][ty][tx] = p2;
@@ -111,7 +108,7 @@ __global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int
             }
             float uc = um1;
             if (a.nonneg && uc < 0.f) uc = 0.f;
-            const float unew = (uc - a.tau * dv + a.lt * fq) * a.inv_onelt;
+            const float unew = pd_primal(uc, a.tau, dv, a.lt, fq, a.onelt);
             const IT v = (IT)k * sxy + col;
             if (CHECK) {
                 const float df = unew - uc;
@@ -119,7 +116,7 @@ __global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int
                 pb += unew * unew;
                 a.ubrk[v] = unew;
             }
-            a.un[v] = unew + a.theta * (unew - uc);
+            a.un[v] = pd_extrapolate(unew, a.theta, uc);
             a.pn[0][v] = p1;
             a.pn[1][v] = p2;
             if (THREE) a.pn[2][v] = p3;

@@ -1,6 +1,7 @@
 // 2.5D streaming PD-TV iteration (pd_tiled.cu).
 #pragma once
 
+#include "pd_math.cuh"
 #include "runtime.cuh"
 
 namespace cilreg {
@@ -12,7 +13,8 @@ struct PdStreamArgs {
     float* pn[3];       // dual (next)
     const float* f;
     float* ubrk;        // U before extrapolation, written on check iterations
-    float sigma, tau, lt, inv_onelt, theta;
+    float sigma, tau, lt, theta;
+    DoubleDivisor onelt;  // the reference's double (1.0 + lt)
     int nonneg, aniso, check;
 };
 

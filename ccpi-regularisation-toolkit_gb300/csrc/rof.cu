@@ -118,6 +118,14 @@ long long rof_partial_slots(const Dims& d) {
     return use_simple_kernel() ? num_blocks(plan_launch(d)) : rof_tiled_plan(d).nblocks;
 }
 
+int rof_check_grid(const Dims& d) {
+    const dim3 g = use_simple_kernel() ? plan_launch(d).grid : rof_tiled_plan(d).grid;
+    if (g.y > 65535u || g.z > 65535u)
+        return fail(ERR_ARG, __FILE__, __LINE__, "shape (%d, %d, %d) exceeds the launch grid (%u x %u x %u CTAs)",
+                    d.nx, d.ny, d.nz, g.x, g.y, g.z);
+    return OK;
+}
+
 int rof_launch_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
                     const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
     if (use_simple_kernel()) {
@@ -137,6 +145,7 @@ int rof_launch_step(const float* cur, float* nxt, const float* f, const float* l
 
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info, const float* u_init) {
+    CILREG_TRY(rof_check_grid(d));
     Scratch scratch(s);
     const long long nparts = rof_partial_slots(d);
     IterControl ctl(s, scratch, iters, epsil, nparts);

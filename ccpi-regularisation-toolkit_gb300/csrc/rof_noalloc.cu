@@ -22,7 +22,10 @@
 //     on it and must be serialised by the caller;
 //   * the first call on each device looks up the array's device address
 //     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture.
+//     before any stream capture;
+//   * a call waits for its stream before it returns (it reads the stop
+//     control back); with epsil != 0 it also reads the stop flag every
+//     twentieth iteration and stops enqueueing once the rule has fired.
 #include <mutex>
 
 #include "../../include/cilreg_gb300.h"
@@ -85,8 +88,7 @@ extern "C" int cilreg_rof_tv_dev_noalloc(const float* d_in, float* d_out, float*
         return fail(ERR_ARG, __FILE__, __LINE__,
                     "%lld voxels exceed the no-allocation limit of %lld voxels (use cilreg_rof_tv_dev)", d.n,
                     kNoAllocMaxVoxels);
-    if ((dimY + 7) / 8 > 65535)
-        return fail(ERR_ARG, __FILE__, __LINE__, "shape (%d, %d, %d) exceeds the launch grid", dimX, dimY, dimZ);
+    CILREG_TRY(rof_check_grid(d));  // the same limit as cilreg_rof_tv_dev, from the plan that runs
     const long long nparts = rof_partial_slots(d);
     if (epsil != 0.0f && nparts > kNoAllocMaxPartials)
         return fail(ERR_ARG, __FILE__, __LINE__,
@@ -109,7 +111,18 @@ extern "C" int cilreg_rof_tv_dev_noalloc(const float* d_in, float* d_out, float*
         const int check = (epsil != 0.0f && (it % 5) == 0) ? 1 : 0;
         CILREG_TRY(rof_launch_step(bufs[it & 1], bufs[(it + 1) & 1], d_in, d_lambda, lambdaPar, tau, d, ctl, check,
                                    partials, s));
-        if (check) CILREG_TRY(launch_finalize_check(partials, nparts, ctl, epsil, it, s));
+        if (check) {
+            CILREG_TRY(launch_finalize_check(partials, nparts, ctl, epsil, it, s));
+            // every fourth check, read the stop flag (a copy into host stack
+            // memory, no allocation) and stop enqueueing iterations that
+            // would only return at once
+            if ((it / 5) % 4 == 3) {
+                int stop = 0;
+                CILREG_CUDA(cudaMemcpyAsync(&stop, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, s));
+                CILREG_CUDA(cudaStreamSynchronize(s));
+                if (stop) break;
+            }
+        }
     }
     if (iters > 0) CILREG_TRY(launch_select_pingpong(ctl, iters, bufs, d_out, d.n, s));
     StopCtl h;

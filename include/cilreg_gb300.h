@@ -2,9 +2,11 @@
  * cilreg_gb300.h — C ABI of the GB300 (sm_103a) proximal regularisers.
  *
  * Drop-in for the CCPi Regularisation Toolkit's shared libraries:
- *   libcilregcuda.so  exports the *_GPU_main family and the cilreg_*_dev API;
- *   libcilreg.so      exports the *_CPU_main family (same object code).
- * Both libraries contain all symbols below.
+ *   libcilregcuda.so  holds every entry point below (the *_GPU_main and
+ *                     *_CPU_main families and the cilreg_* API);
+ *   libcilreg.so      exports the same entry points, each forwarding to
+ *                     libcilregcuda.so in its directory, so that a process
+ *                     binding both names holds one copy of the GPU library.
  *
  * Arrays are C-ordered float32 with dimX the fastest axis: linear index
  * (dimX*dimY)*k + dimX*j + i.  A 2D image has dimZ == 1 (dimZ == 0 is read as 1).
@@ -15,7 +17,8 @@
  * a counter increments when re < epsil and the run stops once it exceeds 3.
  *
  * Return values: 0 on success, negative on failure
- *   -1 CUDA error, -2 invalid argument, -3 no CUDA device, -4 out of device memory;
+ *   -1 CUDA error, -2 invalid argument, -3 no CUDA device, -4 out of device memory,
+ *   -5 cancelled (prox-session outer loops only);
  * the message is available from cilreg_last_error() (per host thread) and is
  * also printed to stderr, as the reference does (regularisers_GPU/shared.h:15-38).
  * All entry points may be called concurrently from several host threads.
@@ -267,7 +270,9 @@ int cilreg_debug_fail_allocations(int n);
  * epsil != 0 at most 2^18 reduction blocks.  All calls share the array:
  * calls whose GPU work overlaps race and must be serialised by the caller.
  * The first call on a device looks up the array's address on that device;
- * make it before any stream capture. */
+ * make it before any stream capture.  A call waits for its stream before it
+ * returns; with epsil != 0 it reads the stop flag every twentieth iteration
+ * and stops enqueueing once the rule has fired. */
 int cilreg_rof_tv_dev_noalloc(const float *d_in, float *d_out, float *infovector, const float *d_lambda,
                               float lambdaPar, int iters, float tau, float epsil, int dimX, int dimY, int dimZ,
                               void *stream);
