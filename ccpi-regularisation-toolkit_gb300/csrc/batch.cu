@@ -1,19 +1,30 @@
 // Batched regularisation of many volumes of uneven shape (FGP-TV and TGV).
 //
-// All volumes advance together: each iteration is ONE kernel launch (two for
-// TGV) over a flat grid holding the tiles of every volume, driven by a
-// device-resident descriptor table (dims, state pointers, lambda, stop
-// control) and a tile -> volume map.  Every volume keeps its own stopping rule
-// (one finalize CTA per volume); the tiles of a stopped volume return at once.
-// With CILREG_BATCH_GRAPH (default) the whole iteration loop is captured into
-// one CUDA graph and launched once.  With CILREG_BATCH_AUTOTUNE the z chunk of
-// the FGP streaming kernel is chosen by timing candidate chunks on the batch
-// itself; choices are kept per process and optionally in a cache file
-// (CILREG_AUTOTUNE_CACHE).
+// All volumes advance together, driven by a device-resident descriptor table
+// (dims, state pointers, lambda, stop control) and a tile -> volume map, and
+// every volume keeps its own stopping rule.  Two schedules:
+//   * graph: each iteration is ONE kernel launch (two for 2D TGV) over a flat
+//     grid of every volume's tiles, a finalize CTA per volume on check
+//     iterations; the whole loop is captured into one CUDA graph and launched
+//     once (CILREG_BATCH_GRAPH=0: plain launches);
+//   * persistent (FGP): one launch runs every iteration of every volume; its
+//     CTAs take (iteration, tile) items from a device-side queue and wait
+//     only for their own volume's previous iteration (k_fgp_persistent,
+//     fgp_tiled.cu), optionally in groups of volumes whose state fits in L2.
+// An autotuner (on by default for 3D FGP batches of 8 or more iterations;
+// CILREG_BATCH_AUTOTUNE=0 turns it off) times three iterations of each
+// candidate schedule and z chunk on the batch itself and keeps the fastest,
+// per GPU name and batch shape, in the process and in a cache file
+// (CILREG_AUTOTUNE_CACHE, default ~/.cache/cilreg-gb300/autotune.tsv; an
+// empty value keeps it in the process only).  CILREG_BATCH_MODE=graph or
+// persistent fixes the schedule ("persistent:<MB>" with volume groups of at
+// most that many MB of state).
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <sys/stat.h>
 
 #include <map>
 #include <mutex>
@@ -77,11 +88,26 @@ std::string tune_key(const char* alg, const BatchLayout& L) {
     return k;
 }
 
+// the autotuner's cache file ("" when the cache stays in the process)
+std::string tune_cache_path() {
+    const char* e = getenv("CILREG_AUTOTUNE_CACHE");
+    if (e) return std::string(e);
+    std::string dir;
+    if (const char* x = getenv("XDG_CACHE_HOME")) dir = x;
+    else if (const char* h = getenv("HOME")) dir = std::string(h) + "/.cache";
+    else return "";
+    mkdir(dir.c_str(), 0755);
+    dir += "/cilreg-gb300";
+    mkdir(dir.c_str(), 0755);
+    return dir + "/autotune.tsv";
+}
+
 int cached_choice(const std::string& key) {
     std::lock_guard<std::mutex> g(g_tune_lock);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second;
-    const char* path = getenv("CILREG_AUTOTUNE_CACHE");
+    const std::string cpath = tune_cache_path();
+    const char* path = cpath.empty() ? nullptr : cpath.c_str();
     if (path) {
         FILE* fp = fopen(path, "r");
         if (fp) {
@@ -106,7 +132,8 @@ int cached_choice(const std::string& key) {
 void store_choice(const std::string& key, int z) {
     std::lock_guard<std::mutex> g(g_tune_lock);
     g_tune[key] = z;
-    const char* path = getenv("CILREG_AUTOTUNE_CACHE");
+    const std::string cpath = tune_cache_path();
+    const char* path = cpath.empty() ? nullptr : cpath.c_str();
     if (path) {
         FILE* fp = fopen(path, "a");
         if (fp) {
@@ -260,6 +287,181 @@ int read_infos(const StopCtl* d_ctl, int nvol, float* infos, cudaStream_t s) {
     return OK;
 }
 
+// One persistent launch for every iteration of every volume.  group_mb > 0
+// cuts the volumes (in order) into groups of at most that much FGP state
+// (44 B per voxel), run one group after another so that a small group's
+// state stays in L2 across its iterations; 0 runs all volumes as one group.
+// Items of iterations it0 .. it0 + nits - 1 of a run of `iters`; with
+// ran_out, a wait that gives up is reported there instead of failing.
+int fgp_persistent_enqueue(FgpBatch& B, const BatchLayout& L, int it0, int nits, int iters, float epsil,
+                           int methodTV, int nonneg, int group_mb, long long wait_limit, cudaStream_t s, Scratch& sc,
+                           int* ran_out = nullptr) {
+    const int nvol = (int)L.dims.size();
+    std::vector<long long> gtile{0}, gitem{0};
+    double acc = 0.0;
+    for (int v = 0; v < nvol; v++) {
+        const double bytes = 44.0 * (double)L.dims[v].n;
+        if (group_mb > 0 && acc > 0.0 && acc + bytes > (double)group_mb * 1048576.0) {
+            gtile.push_back(B.vols[v].tile_base);
+            gitem.push_back(gitem.back() + (long long)nits * (gtile.back() - gtile[gtile.size() - 2]));
+            acc = 0.0;
+        }
+        acc += bytes;
+    }
+    gtile.push_back(B.ntiles);
+    gitem.push_back(gitem.back() + (long long)nits * (gtile.back() - gtile[gtile.size() - 2]));
+    const int ngroups = (int)gtile.size() - 1;
+    std::vector<float> carr(iters > 0 ? iters : 1);
+    float tk = 1.0f, cprev = 0.0f;
+    for (int it = 0; it < iters; it++) {
+        carr[it] = cprev;
+        const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;  // FGP_TV_core.c:138
+        cprev = (tk - 1.0f) / tkp1;
+        tk = tkp1;
+    }
+    // queue counter, error flag, per-volume arrivals and releases: zeroed together
+    const size_t ctl_bytes = align256(sizeof(unsigned long long) * (1 + (size_t)nvol) + sizeof(int) * (1 + (size_t)nvol));
+    unsigned char* ctl = (unsigned char*)sc.bytes(ctl_bytes);
+    float* d_carr = sc.floats(iters > 0 ? iters : 1);
+    long long* d_g = (long long*)sc.bytes(sizeof(long long) * 2 * (size_t)(ngroups + 1));
+    if (!ctl || !d_carr || !d_g) return sc.status();
+    CILREG_CUDA(cudaMemsetAsync(ctl, 0, ctl_bytes, s));
+    std::vector<long long> g(gtile);
+    g.insert(g.end(), gitem.begin(), gitem.end());
+    CILREG_CUDA(cudaMemcpyAsync(d_carr, carr.data(), sizeof(float) * carr.size(), cudaMemcpyHostToDevice, s));
+    CILREG_CUDA(cudaMemcpyAsync(d_g, g.data(), sizeof(long long) * g.size(), cudaMemcpyHostToDevice, s));
+    FgpPersistArgs A;
+    A.vols = B.d_vols;
+    A.tile_vol = B.d_tile_vol;
+    A.carr = d_carr;
+    A.next = (unsigned long long*)ctl;
+    A.arrive = A.next + 1;
+    A.error = (int*)(A.arrive + nvol);
+    A.release = A.error + 1;
+    A.gtile = d_g;
+    A.gitem = d_g + (ngroups + 1);
+    A.ngroups = ngroups;
+    A.it0 = it0;
+    A.iters = iters;
+    A.nonneg = nonneg == 1;
+    A.aniso = methodTV != 0;
+    A.checking = epsil != 0.0f;
+    A.epsil = epsil;
+    A.wait_limit = wait_limit;
+    const long long items = gitem.back();
+    int nctas = fgp_persistent_ctas();
+    if ((long long)nctas > items) nctas = (int)items;
+    if (items > 0) {
+        CILREG_TRY(fgp_persistent_launch(A, L.three, B.wide, nctas, s));
+        note_launch();
+    }
+    int h_err = 0;
+    CILREG_CUDA(cudaMemcpyAsync(&h_err, A.error, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    // the host buffers must outlive their copies, done by the synchronisation above
+    if (ran_out) {
+        *ran_out = h_err;
+        return OK;
+    }
+    if (h_err) return fail(ERR_CUDA, __FILE__, __LINE__, "persistent batch: a dependency wait ran out");
+    return OK;
+}
+
+// schedule of a batched FGP run; code = mode * 100000 + group_mb * 100 + zc
+struct FgpSchedule {
+    int mode = 0;      // 0 graph of flat-grid launches, 1 persistent kernel
+    int zc = 0;        // z chunk of the streaming tiles (0: fgp_default_zchunk)
+    int group_mb = 0;  // persistent: L2 groups of at most this many MB of state (0: one group)
+    int code() const { return mode * 100000 + group_mb * 100 + zc; }
+    static FgpSchedule from(int c) {
+        FgpSchedule t;
+        t.mode = c / 100000;
+        t.group_mb = (c / 100) % 1000;
+        t.zc = c % 100;
+        return t;
+    }
+};
+
+constexpr long long kWaitLimit = 1LL << 23;  // polls of about 0.2 us: well over a second
+
+int fgp_run_schedule(const FgpSchedule& S, const BatchLayout& L, const float* const* f, float* const* u,
+                     const float* lams, int iters, float epsil, int methodTV, int nonneg, float* infos,
+                     cudaStream_t s) {
+    const int nvol = (int)L.dims.size();
+    Scratch sc(s);
+    FgpBatch B;
+    CILREG_TRY(fgp_build(B, sc, L, f, u, lams, S.zc, s));
+    CILREG_TRY(fgp_reset(B, nvol, iters, s));
+    if (S.mode == 1 && iters > 0)
+        CILREG_TRY(fgp_persistent_enqueue(B, L, 0, iters, iters, epsil, methodTV, nonneg, S.group_mb, kWaitLimit, s,
+                                          sc));
+    else if (env_flag("CILREG_BATCH_GRAPH", true) && iters > 0)
+        CILREG_TRY(run_graph(s, [&]() { return fgp_enqueue(B, nvol, L.three, iters, epsil, methodTV, nonneg, s); }));
+    else
+        CILREG_TRY(fgp_enqueue(B, nvol, L.three, iters, epsil, methodTV, nonneg, s));
+    return read_infos(B.d_ctl, nvol, infos, s);
+}
+
+// pick the schedule: fixed by CILREG_BATCH_MODE, else the cached or freshly
+// timed fastest candidate for 3D batches, else one graph of launches
+int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* const* u, const float* lams, int iters,
+                        int methodTV, int nonneg, cudaStream_t s, FgpSchedule& out) {
+    out = FgpSchedule();
+    if (const char* m = getenv("CILREG_BATCH_MODE")) {
+        // "graph", "persistent" or "persistent:<MB>" (volume groups of at most MB of state)
+        if (m[0] == 'p') {
+            out.mode = 1;
+            if (const char* c = strchr(m, ':')) out.group_mb = atoi(c + 1) < 0 ? 0 : atoi(c + 1) % 1000;
+        }
+        return OK;
+    }
+    if (!L.three || iters < 8 || !env_flag("CILREG_BATCH_AUTOTUNE", true)) return OK;
+    const std::string key = tune_key("fgp-schedule", L);
+    const int c = cached_choice(key);
+    if (c != 0) {
+        out = FgpSchedule::from(c);
+        return OK;
+    }
+    std::vector<FgpSchedule> cand;
+    for (int mode = 0; mode < 2; mode++)
+        for (int zc : {64, 32, 16}) {
+            FgpSchedule t;
+            t.mode = mode;
+            t.zc = zc;
+            cand.push_back(t);
+        }
+    FgpSchedule grouped;
+    grouped.mode = 1;
+    grouped.zc = 16;
+    grouped.group_mb = 96;
+    cand.push_back(grouped);
+    float best = 1e30f;
+    cudaEvent_t e0, e1;
+    CILREG_CUDA(cudaEventCreate(&e0));
+    CILREG_CUDA(cudaEventCreate(&e1));
+    int rc = OK;
+    for (const FgpSchedule& t : cand) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && rc == OK; rep++) {  // the first run also warms the pool
+            cudaEventRecord(e0, s);
+            rc = fgp_run_schedule(t, L, f, u, lams, 3, 0.0f, methodTV, nonneg, nullptr, s);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (rc != OK) break;
+        if (ms < best) {
+            best = ms;
+            out = t;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CILREG_TRY(rc);
+    store_choice(key, out.code());
+    return OK;
+}
+
 int fgp_batch_run(int nvol, const float* const* f, float* const* u, const int* dims, const float* lams, int iters,
                   float epsil, int methodTV, int nonneg, float* infos, cudaStream_t caller) {
     BatchLayout L;
@@ -272,49 +474,9 @@ int fgp_batch_run(int nvol, const float* const* f, float* const* u, const int* d
     CILREG_TRY(use_device(dev));
     CILREG_CUDA(cudaStreamSynchronize(caller));  // inputs written on the caller's stream are ready
     cudaStream_t s = thread_stream(dev);
-    Scratch sc(s);
-
-    int zc = 0;
-    if (L.three && env_flag("CILREG_BATCH_AUTOTUNE", false) && iters >= 8) {
-        const std::string key = tune_key("fgp", L);
-        zc = cached_choice(key);
-        if (zc == 0) {
-            // time three iterations for each candidate chunk on the batch itself
-            const int cand[3] = {16, 32, 64};
-            float best = 1e30f;
-            for (int c : cand) {
-                Scratch tsc(s);
-                FgpBatch T;
-                CILREG_TRY(fgp_build(T, tsc, L, f, u, lams, c, s));
-                CILREG_TRY(fgp_reset(T, nvol, 3, s));
-                cudaEvent_t e0, e1;
-                cudaEventCreate(&e0);
-                cudaEventCreate(&e1);
-                cudaEventRecord(e0, s);
-                CILREG_TRY(fgp_enqueue(T, nvol, true, 3, 0.0f, methodTV, nonneg, s));
-                cudaEventRecord(e1, s);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                if (ms < best) {
-                    best = ms;
-                    zc = c;
-                }
-            }
-            store_choice(key, zc);
-        }
-    }
-
-    FgpBatch B;
-    CILREG_TRY(fgp_build(B, sc, L, f, u, lams, zc, s));
-    CILREG_TRY(fgp_reset(B, nvol, iters, s));
-    if (env_flag("CILREG_BATCH_GRAPH", true) && iters > 0)
-        CILREG_TRY(run_graph(s, [&]() { return fgp_enqueue(B, nvol, L.three, iters, epsil, methodTV, nonneg, s); }));
-    else
-        CILREG_TRY(fgp_enqueue(B, nvol, L.three, iters, epsil, methodTV, nonneg, s));
-    return read_infos(B.d_ctl, nvol, infos, s);
+    FgpSchedule S;
+    CILREG_TRY(fgp_choose_schedule(L, f, u, lams, iters, methodTV, nonneg, s, S));
+    return fgp_run_schedule(S, L, f, u, lams, iters, epsil, methodTV, nonneg, infos, s);
 }
 
 // --------------------------------------------------------------------------
@@ -582,6 +744,36 @@ int cilreg_fgp_tv_batch_dev(int nvol, const float* const* d_in, float* const* d_
                             void* stream) {
     return fgp_batch_run(nvol, d_in, d_out, dims, lambdas, iters, epsil, methodTV, nonneg, infovectors,
                          (cudaStream_t)stream);
+}
+
+int cilreg_selftest_batch_wait(int gpu_device, int* ran_out) {
+    if (!ran_out) return fail(ERR_ARG, __FILE__, __LINE__, "null result pointer");
+    *ran_out = 0;
+    CILREG_TRY(use_device(gpu_device));
+    cudaStream_t s = thread_stream(gpu_device);
+    Scratch sc(s);
+    const int dims[3] = {40, 20, 12};
+    BatchLayout L;
+    CILREG_TRY(read_dims(1, dims, L));
+    const long long n = L.dims[0].n;
+    float* f = sc.floats(2 * n);
+    if (!f) return sc.status();
+    float* u = f + n;
+    CILREG_CUDA(cudaMemsetAsync(f, 0, sizeof(float) * 2 * n, s));
+    const float lam = 0.05f;
+    FgpBatch B;
+    CILREG_TRY(fgp_build(B, sc, L, &f, &u, &lam, 0, s));
+    CILREG_TRY(fgp_reset(B, 1, 2, s));
+    // every item of this launch belongs to iteration 1, whose predecessor is
+    // never released: each wait polls 4096 times (about a millisecond), gives
+    // up, flags the error and its CTA leaves
+    int out = 0;
+    CILREG_TRY(fgp_persistent_enqueue(B, L, 1, 1, 2, 0.0f, 0, 0, 0, 4096, s, sc, &out));
+    // the device still runs work
+    CILREG_TRY(fgp_reset(B, 1, 2, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
+    *ran_out = out;
+    return OK;
 }
 
 int cilreg_tgv_batch_dev(int nvol, const float* const* d_in, float* const* d_out, const int* dims,

@@ -52,7 +52,16 @@ struct TiledArgs {
 // DTV: the FGP-dTV iteration (FGP_dTV_core.c:92-120): R and the gradient of U
 // are projected onto the orthogonal complement of a.b at each voxel
 // (ProjectVect_func, Grad_dfunc: FGP_dTV_core.c:302-363).
-template <bool THREE, bool CHECK, typename IT, bool DTV = false>
+// Loads of state the same kernel may have written: through L2 only (the SM's
+// L1 is not coherent with other SMs' stores) in the persistent kernel, which
+// runs every iteration in one launch; the read-only path otherwise.
+template <bool COHERENT>
+__device__ __forceinline__ float ld_state(const float* p) {
+    if constexpr (COHERENT) return __ldcg(p);
+    else return __ldg(p);
+}
+
+template <bool THREE, bool CHECK, typename IT, bool DTV = false, bool COHERENT = false>
 __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& d, int zc, int bx, int by, int bz,
                                                 float& pa_out, float& pb_out) {
     __shared__ float sR1[BY][BX];
@@ -76,13 +85,13 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
     auto load_plane = [&](int k) {
         if (in_xy && k >= 0 && k < nz) {
             const IT v = (IT)k * sxy + col;
-            c1 = __ldg(a.pc[0] + v);
-            o1 = __ldg(a.po[0] + v);
-            c2 = __ldg(a.pc[1] + v);
-            o2 = __ldg(a.po[1] + v);
+            c1 = ld_state<COHERENT>(a.pc[0] + v);
+            o1 = ld_state<COHERENT>(a.po[0] + v);
+            c2 = ld_state<COHERENT>(a.pc[1] + v);
+            o2 = ld_state<COHERENT>(a.po[1] + v);
             if (THREE) {
-                c3 = __ldg(a.pc[2] + v);
-                o3 = __ldg(a.po[2] + v);
+                c3 = ld_state<COHERENT>(a.pc[2] + v);
+                o3 = ld_state<COHERENT>(a.po[2] + v);
             }
             fv = __ldg(a.f + v);
             if (DTV) {
@@ -120,7 +129,10 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
         // U_prev of plane k, consumed one plane later: loaded here so that its
         // latency overlaps the barriers instead of stalling the P step
         float uo_next = 0.f;
-        if (CHECK && p_pt && k >= z0 && k < z1) uo_next = a.u[(IT)k * sxy + col];
+        if (CHECK && p_pt && k >= z0 && k < z1) {
+            if constexpr (COHERENT) uo_next = __ldcg(a.u + (IT)k * sxy + col);
+            else uo_next = a.u[(IT)k * sxy + col];
+        }
         sR1[ty][tx] = r1;
         sR2[ty][tx] = r2;
         __syncthreads();
@@ -241,7 +253,190 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* _
     if (CHECK) block_pair_partial<NT>(pa, pb, V.partials, lt);
 }
 
+// --------------------------------------------------------------------------
+// Persistent batched FGP: every iteration of every volume in one launch.
+//
+// Work items are (iteration, tile) pairs of a group of volumes, handed out by
+// an atomic counter in iteration-major order within each group, groups one
+// after another.  An item of iteration `it` waits until its volume's
+// iteration it-1 is released, i.e. all that volume's tiles of it-1 have
+// finished and, on a stopping-check iteration, the volume's check has run.
+// Every dependency of an item was handed out before it, to a CTA that is
+// running, so the waits always end (no co-residency of the grid is needed).
+// A wait still gives up after `wait_limit` polls, sets *error and leaves; the
+// host then fails the call.  The last tile to finish an iteration of a volume
+// runs that volume's stopping check (the same fixed-order FP64 reduction as
+// the finalize kernel) and releases the iteration.  State written within the
+// launch is read through L2 (ld.global.cg), never from a stale L1 line.
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// one volume's stopping check by the whole CTA (NT = 512 threads): the sums of
+// k_finalize_batch's 1024-thread order (thread t and t + 512 of that kernel
+// are this thread's two chains), so the relative change is bit-identical
+__device__ __forceinline__ void persistent_check(const FgpBatchVol& V, long long ntiles, float epsil, int it) {
+    const int tid = threadIdx.x + BX * threadIdx.y;
+    double a0 = 0.0, b0 = 0.0, a1 = 0.0, b1 = 0.0;
+    for (long long p = tid; p < ntiles; p += 1024) {
+        const double2 w = __ldcg(V.partials + p);
+        a0 += w.x;
+        b0 += w.y;
+    }
+    for (long long p = tid + 512; p < ntiles; p += 1024) {
+        const double2 w = __ldcg(V.partials + p);
+        a1 += w.x;
+        b1 += w.y;
+    }
+    __shared__ double sa[32], sb[32];
+    a0 = warp_sum(a0);
+    b0 = warp_sum(b0);
+    a1 = warp_sum(a1);
+    b1 = warp_sum(b1);
+    if ((tid & 31) == 0) {
+        sa[tid >> 5] = a0;
+        sb[tid >> 5] = b0;
+        sa[16 + (tid >> 5)] = a1;
+        sb[16 + (tid >> 5)] = b1;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        const double a = warp_sum(sa[tid]);
+        const double b = warp_sum(sb[tid]);
+        if (tid == 0) {
+            StopCtl* c = V.ctl;
+            const float re = sqrtf((float)a) / sqrtf((float)b);
+            c->re = re;
+            if (re < epsil) c->count += 1;
+            if (c->count > 3) {
+                c->stop = 1;
+                c->iters = it;
+            }
+        }
+    }
+}
+
+template <bool THREE, typename IT>
+__global__ void __launch_bounds__(NT, 3) k_fgp_persistent(FgpPersistArgs A) {
+    __shared__ long long s_item;
+    __shared__ int s_flag, s_stop;
+    const int tid = threadIdx.x + BX * threadIdx.y;
+    const long long total = A.gitem[A.ngroups];
+    for (;;) {
+        if (tid == 0) s_item = (long long)atomicAdd(A.next, 1ULL);
+        __syncthreads();
+        const long long i = s_item;
+        if (i >= total) break;
+        int lo = 0, hi = A.ngroups - 1;  // the group holding item i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.gitem[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const long long gt0 = A.gtile[lo], nt_group = A.gtile[lo + 1] - gt0;
+        const long long r = i - A.gitem[lo];
+        const int it = A.it0 + (int)(r / nt_group);
+        const long long t = gt0 + r % nt_group;
+        const int v = A.tile_vol[t];
+        const FgpBatchVol& V = A.vols[v];
+        const long long ntv = (long long)V.gx * V.gy * V.gz;
+        if (tid == 0) {
+            int fl = 0;
+            long long polls = 0;
+            while (ld_acquire_gpu(A.release + v) < it) {
+                if (ld_acquire_gpu(A.error) != 0 || ++polls > A.wait_limit) {
+                    atomicExch(A.error, 1);
+                    fl = 1;
+                    break;
+                }
+                __nanosleep(200);
+            }
+            s_flag = fl;
+            // read once, after the release: the flag of a check iteration
+            // before `it` is final by then
+            s_stop = fl ? 0 : ld_acquire_gpu(&V.ctl->stop);
+        }
+        __syncthreads();
+        if (s_flag) break;  // a wait gave up (or another CTA's did): leave, the host reports it
+        const bool stopped = s_stop != 0;
+        const int check = (A.checking && it % 5 == 0) ? 1 : 0;
+        const long long lt = t - V.tile_base;
+        if (!stopped) {
+            TiledArgs a;
+            for (int q = 0; q < 3; q++) {
+                a.pn[q] = V.ring[it % 3][q];
+                a.pc[q] = V.ring[(it + 2) % 3][q];
+                a.po[q] = V.ring[(it + 1) % 3][q];
+            }
+            a.f = V.f;
+            a.u = V.u;
+            a.lam = V.lam;
+            a.c = A.carr[it];
+            a.multip = V.multip;
+            a.nonneg = A.nonneg;
+            a.aniso = A.aniso;
+            a.write_u = (it == A.iters - 1) || check || (A.checking && (it + 1) % 5 == 0);
+            a.write_p = (it != A.iters - 1);
+            a.check = check;
+            a.b[0] = a.b[1] = a.b[2] = nullptr;
+            a.carr = nullptr;
+            a.cbase = nullptr;
+            a.coff = 0;
+            const int bx = (int)(lt % V.gx);
+            const int by = (int)((lt / V.gx) % V.gy);
+            const int bz = (int)(lt / ((long long)V.gx * V.gy));
+            float pa = 0.f, pb = 0.f;
+            if (check) {
+                fgp_stream_tile<THREE, true, IT, false, true>(a, V.d, V.zc, bx, by, bz, pa, pb);
+                block_pair_partial<NT>(pa, pb, V.partials, lt);
+            } else {
+                fgp_stream_tile<THREE, false, IT, false, true>(a, V.d, V.zc, bx, by, bz, pa, pb);
+            }
+        }
+        __syncthreads();  // the tile's stores are issued and its shared memory is free
+        if (tid == 0) {
+            __threadfence();
+            const unsigned long long done = atomicAdd(A.arrive + v, 1ULL) + 1ULL;
+            __threadfence();
+            s_flag = (done == (unsigned long long)ntv * (unsigned long long)(it - A.it0 + 1)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_flag) {  // the last tile of iteration `it` of volume v
+            if (check && !stopped) persistent_check(V, ntv, A.epsil, it);
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release_gpu(A.release + v, it + 1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+int fgp_persistent_launch(const FgpPersistArgs& A, bool three, bool wide, int nctas, cudaStream_t s) {
+    if (nctas < 1) return fail(ERR_ARG, __FILE__, __LINE__, "no CTAs for the persistent batch");
+    const dim3 block(BX, BY, 1);
+    decltype(&k_fgp_persistent<true, int>) kern;
+    if (!wide) kern = three ? k_fgp_persistent<true, int> : k_fgp_persistent<false, int>;
+    else kern = three ? k_fgp_persistent<true, long long> : k_fgp_persistent<false, long long>;
+    kern<<<nctas, block, 0, s>>>(A);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int fgp_persistent_ctas() {
+    static const int resident = resident_ctas(k_fgp_persistent<true, int>, NT);
+    return sm_count() * resident;
+}
 
 void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz) {
     gx = (d.nx + OX - 1) / OX;

@@ -74,6 +74,28 @@ struct FgpBatchVol {
     int gx, gy, gz, zc;  // tile grid and z chunk of this volume
 };
 
+// Persistent batched run (one launch for every iteration of every volume):
+// the device-side work queue and dependency counters of k_fgp_persistent.
+struct FgpPersistArgs {
+    const FgpBatchVol* vols;
+    const int* tile_vol;
+    const float* carr;          // momentum coefficient of each iteration
+    unsigned long long* next;   // work-item counter (zero before the launch)
+    unsigned long long* arrive; // per volume: tiles finished since it0
+    int* release;               // per volume: iterations released (it0 before the launch)
+    int* error;                 // set when a dependency wait ran out
+    const long long* gtile;     // group g holds flat tiles [gtile[g], gtile[g+1])
+    const long long* gitem;     // group g's first work item; gitem[ngroups] = all items
+    int ngroups;
+    int it0, iters;             // iterations it0 .. it0 + (items of a group) / (its tiles) - 1 of `iters`
+    int nonneg, aniso, checking;
+    float epsil;
+    long long wait_limit;       // polls (about 0.2 us each) before a wait gives up
+};
+int fgp_persistent_launch(const FgpPersistArgs& A, bool three, bool wide, int nctas, cudaStream_t s);
+// CTAs of the persistent kernel resident on the device at once
+int fgp_persistent_ctas();
+
 // tile grid of one volume for the streaming kernel with z chunk `zc`
 void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz);
 

@@ -298,6 +298,12 @@ int cilreg_release_cached(int gpu_device);
  * try limit, as it must, and the device then still ran a kernel.  0 or a
  * negative status. */
 int cilreg_selftest_wait_limit(int gpu_device, int *ran_out);
+/* Self-test of the bounded dependency waits of the persistent batched FGP
+ * kernel: a launch whose work items all wait for an iteration that is never
+ * released.  *ran_out = 1 when the waits gave up after their poll limit and
+ * the call reported it, and the device then still ran work.  0 or a
+ * negative status. */
+int cilreg_selftest_batch_wait(int gpu_device, int *ran_out);
 
 #ifdef __cplusplus
 }

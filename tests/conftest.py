@@ -17,6 +17,15 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session", autouse=True)
+def _autotune_cache_in_tmp(tmp_path_factory):
+    """The batch autotuner's file cache goes to a temporary directory, not the
+    user's home, while the tests run."""
+    if "CILREG_AUTOTUNE_CACHE" not in os.environ:
+        os.environ["CILREG_AUTOTUNE_CACHE"] = str(tmp_path_factory.mktemp("tune") / "autotune.tsv")
+    yield
+
+
+@pytest.fixture(scope="session", autouse=True)
 def _built_oracle():
     """The oracle port is test infrastructure: (re)build it once per session."""
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)

@@ -99,6 +99,48 @@ def test_fgp_batch_autotuned_chunks(monkeypatch, tmp_path):
         assert torch.max(torch.abs(x - y)).item() <= rel_tol(y.cpu().numpy(), 1e-6)
 
 
+@pytest.mark.parametrize("shapes", [SHAPES_3D, SHAPES_2D], ids=["3d", "2d"])
+@pytest.mark.parametrize("epsil", [0.0, 3e-4])
+@pytest.mark.parametrize("mode", ["persistent", "persistent:1"], ids=["one-group", "l2-groups"])
+def test_fgp_persistent_batch_equals_single_calls(shapes, epsil, mode, monkeypatch):
+    """The persistent kernel (every iteration of every volume in one launch,
+    per-volume dependency waits; with 1 MB groups, one volume after another)
+    gives the single-call results bit for bit and the same stopping
+    iterations."""
+    from ccpi.filters.batch import FGP_TV_batch
+    from ccpi.filters.regularisers import FGP_TV
+
+    vols = _volumes(shapes, 9)
+    lams = [0.03 + 0.01 * i for i in range(len(vols))]
+    monkeypatch.setenv("CILREG_BATCH_MODE", mode)
+    infos = np.zeros((len(vols), 2), np.float32)
+    outs = FGP_TV_batch(vols, lams, 60, epsil, 0, 1, infovectors=infos)
+    for v, o, lam, inf in zip(vols, outs, lams, infos):
+        ref_info = np.zeros(2, np.float32)
+        ref = FGP_TV(v, lam, 60, epsil, 0, 1, device="gpu", infovector=ref_info)
+        assert int(inf[0]) == int(ref_info[0])
+        np.testing.assert_array_equal(o, ref)
+
+
+def test_fgp_persistent_batch_on_the_seeded_batch_equals_graph(monkeypatch):
+    """Sixteen uneven volumes of the seeded batch, 40 iterations: the
+    persistent schedule (one group and 96 MB groups) equals the graph of
+    flat-grid launches bit for bit."""
+    import torch
+    from ccpi.filters.batch import FGP_TV_batch
+
+    rng = np.random.default_rng(2)
+    shapes = rng.choice([96, 128, 160, 192, 256], size=(16, 3))
+    vols = [torch.from_numpy(v).cuda() for v in _volumes([tuple(int(e) for e in sh) for sh in shapes], 4)]
+    monkeypatch.setenv("CILREG_BATCH_MODE", "graph")
+    ref = FGP_TV_batch(vols, 0.03, 40, 0.0, 0, 1)
+    for mode in ("persistent", "persistent:96"):
+        monkeypatch.setenv("CILREG_BATCH_MODE", mode)
+        got = FGP_TV_batch(vols, 0.03, 40, 0.0, 0, 1)
+        for a, b in zip(got, ref):
+            assert torch.equal(a, b), mode
+
+
 def test_batch_rejects_mixed_dimensionality():
     from ccpi.filters.batch import FGP_TV_batch
 

@@ -36,3 +36,24 @@ def test_wait_runs_out_and_the_device_stays_usable():
     x = np.random.default_rng(3).random((12, 20, 24)).astype(np.float32)
     out = FGP_TV(x, 0.05, 10, 0.0, 0, 1, device="gpu")
     assert np.isfinite(out).all()
+
+
+def test_persistent_batch_wait_runs_out_and_the_device_stays_usable():
+    """The persistent batched kernel's dependency waits: a launch whose work
+    items all wait for an iteration that is never released gives up after
+    its poll limit, reports it, and the device keeps working."""
+    from ccpi.filters.batch import FGP_TV_batch
+
+    lib = ctypes.CDLL(os.path.join(PKG, "ccpi", "filters", "libcilregcuda.so"))
+    lib.cilreg_selftest_batch_wait.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.cilreg_selftest_batch_wait.restype = ctypes.c_int
+    lib.cilreg_last_error.restype = ctypes.c_char_p
+    ran_out = ctypes.c_int(-1)
+    t0 = time.perf_counter()
+    st = lib.cilreg_selftest_batch_wait(0, ctypes.byref(ran_out))
+    assert st == 0, lib.cilreg_last_error()
+    assert ran_out.value == 1
+    assert time.perf_counter() - t0 < 60.0
+    vols = [np.random.default_rng(4).random((10, 12, 14)).astype(np.float32) for _ in range(3)]
+    outs = FGP_TV_batch(vols, 0.05, 12)
+    assert all(np.isfinite(o).all() for o in outs)
