@@ -863,6 +863,25 @@ def main():
     e2e_t_max, e2e_vi_all = reduce_over_ranks(pg, e2e_t, e2e_vi, dev)
     e2e_val = e2e_vi_all / e2e_t_max
 
+    # the same through the reference-facing Python call with pageable numpy
+    # arrays, as the reference's callers make it (TV.py:524-565): a fresh
+    # output array per call, infovector returned, copies inside the call
+    from ccpi.filters.regularisers import FGP_TV
+
+    info_py = np.zeros(2, np.float32)
+    FGP_TV(x, LAM, MAX_ITERS, EPSIL, METHOD, NONNEG, device="gpu", infovector=info_py)
+    barrier()
+    py_vi, py_times = 0, []
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        out_py = FGP_TV(x, LAM, MAX_ITERS, EPSIL, METHOD, NONNEG, device="gpu", infovector=info_py)
+        py_times.append(time.perf_counter() - t0)
+        py_vi += n * int(info_py[0])
+    barrier()
+    if not bool(np.isfinite(out_py).all()) or float(np.abs(out_py).max()) == 0.0:
+        raise RuntimeError("the Python-API call left its output empty or non-finite")
+    py_t_max, py_vi_all = reduce_over_ranks(pg, sum(py_times), py_vi, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, kind, cores, dt = cpu_baseline(x, args.cpu_iters)
@@ -884,6 +903,10 @@ def main():
             "cpu_baseline": cpu,
             # the input goes up, the result comes back (U_prev of iteration 0 is zeroed on the device)
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n},
+            "e2e_python_api": {"value": py_vi_all / py_t_max, "unit": UNIT, "h2d_bytes_per_step": 4 * n,
+                               "d2h_bytes_per_step": 4 * n, "ms_per_call": [1e3 * t for t in py_times],
+                               "how": "ccpi.filters.regularisers.FGP_TV(numpy array, device='gpu'): pageable "
+                                      "host arrays, a new output array per call"},
             "gpu_launches": launches,
             "clocks": clock_info,
         }

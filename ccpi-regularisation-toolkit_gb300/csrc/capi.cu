@@ -10,8 +10,13 @@
 // Every entry point validates its arguments, returns a status instead of
 // printing and continuing, and is safe to call from several host threads
 // (each thread gets its own stream; scratch is stream-ordered).
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/mman.h>
+#include <unistd.h>
+
+#include <thread>
 
 #include "../../include/cilreg_gb300.h"
 #include "drivers.cuh"
@@ -37,8 +42,26 @@ int default_device() {
     return e ? atoi(e) : 0;
 }
 
+// Map every page of the caller's output buffer for writing, without changing
+// its contents (MADV_POPULATE_WRITE).  A freshly allocated host array (numpy
+// zeros_like, calloc) is backed by pages that only fault in when first
+// written; the download would otherwise take those faults itself, tens of
+// milliseconds per 512 MiB.  Runs on a helper thread while the GPU iterates.
+void populate_for_write(void* p, size_t bytes) {
+#ifdef MADV_POPULATE_WRITE
+    const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t a = (uintptr_t)p & ~(uintptr_t)(page - 1);
+    const uintptr_t e = ((uintptr_t)p + bytes + page - 1) & ~(uintptr_t)(page - 1);
+    madvise((void*)a, e - a, MADV_POPULATE_WRITE);  // best effort: an error leaves the faults to the copy
+#else
+    (void)p;
+    (void)bytes;
+#endif
+}
+
 // Host-pointer wrapper: upload input (and the output buffer when `upload_out`),
-// run `body(d_in, d_out, stream)`, download the output.
+// run `body(d_in, d_out, stream)`, download the output.  Outputs of 16 MiB or
+// more are populated for writing on a helper thread meanwhile.
 template <class Body>
 int host_call(const float* in, float* out, int dev, const Dims& d, bool upload_out, Body body) {
     if (!in || !out) return fail(ERR_ARG, __FILE__, __LINE__, "null Input/Output pointer");
@@ -53,7 +76,10 @@ int host_call(const float* in, float* out, int dev, const Dims& d, bool upload_o
         const size_t bytes = sizeof(float) * (size_t)d.n;
         CILREG_CUDA(cudaMemcpyAsync(d_in, in, bytes, cudaMemcpyHostToDevice, s));
         if (upload_out) CILREG_CUDA(cudaMemcpyAsync(d_out, out, bytes, cudaMemcpyHostToDevice, s));
+        std::thread pre;
+        if (bytes >= (16u << 20)) pre = std::thread(populate_for_write, (void*)out, bytes);
         rc = body(d_in, d_out, s);
+        if (pre.joinable()) pre.join();
         if (rc == 0) {
             CILREG_CUDA(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, s));
             CILREG_CUDA(cudaStreamSynchronize(s));

@@ -6,7 +6,6 @@
 namespace cilreg {
 
 struct D4Plan {
-    int cols = 0;  // the 3D column kernel's rows per thread (0: one voxel per thread)
     dim3 grid, block;
     long long nblocks = 0;
     int zchunk = 0;

@@ -513,3 +513,4 @@ def test_diff4th_streaming_kernel_equals_per_voxel_kernels(shape, monkeypatch):
         monkeypatch.delenv("CILREG_D4_KERNEL")
         assert int(ia[0]) == int(ib[0])
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
