@@ -36,6 +36,7 @@
 #include "fgp_tiled.cuh"
 #include "tgv_batch.cuh"
 #include "tgv_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -251,6 +252,7 @@ int fgp_enqueue(FgpBatch& B, int nvol, bool three, int iters, float epsil, int m
 // run the enqueued loop through one CUDA graph (capture, instantiate, launch)
 template <class Enq>
 int run_graph(cudaStream_t s, Enq enqueue) {
+    CILREG_RANGE("cilreg graph launch");
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     CILREG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -464,6 +466,7 @@ int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* cons
 
 int fgp_batch_run(int nvol, const float* const* f, float* const* u, const int* dims, const float* lams, int iters,
                   float epsil, int methodTV, int nonneg, float* infos, cudaStream_t caller) {
+    CILREG_RANGE("cilreg FGP-TV batch");
     BatchLayout L;
     CILREG_TRY(read_dims(nvol, dims, L));
     if (!f || !u || !lams) return fail(ERR_ARG, __FILE__, __LINE__, "null batch arrays");
@@ -615,6 +618,7 @@ int tgv_batch_run_fused(int nvol, const float* const* f, float* const* u, const 
 // TGV batch
 int tgv_batch_run(int nvol, const float* const* f, float* const* u, const int* dims, const float* lams, float alpha1,
                   float alpha0, int iters, float L2, float epsil, float* infos, cudaStream_t caller) {
+    CILREG_RANGE("cilreg TGV batch");
     BatchLayout L;
     CILREG_TRY(read_dims(nvol, dims, L));
     if (!f || !u || !lams) return fail(ERR_ARG, __FILE__, __LINE__, "null batch arrays");

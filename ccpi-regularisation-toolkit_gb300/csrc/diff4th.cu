@@ -8,6 +8,7 @@
 #include "drivers.cuh"
 
 #include <stdlib.h>
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(256) k_d4_update(float* __restrict__ U, const 
 
 int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, float epsil,
                 const Dims& d, cudaStream_t s, float* info) {
+    CILREG_RANGE("cilreg Diff4th");
     const bool three = d.nz > 1;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);

@@ -13,6 +13,7 @@
 
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(256) k_dtv_gradnorm(const float* __restrict__ 
 
 int dtv_run(const float* f, const float* ref, float* u_out, float lam, int iters, float epsil, float eta,
             int methodTV, int nonneg, const Dims& d, cudaStream_t s, float* info) {
+    CILREG_RANGE("cilreg FGP-dTV");
     if (!ref) return fail(ERR_ARG, __FILE__, __LINE__, "null reference image");
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;

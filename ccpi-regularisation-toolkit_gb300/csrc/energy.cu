@@ -12,6 +12,7 @@
 
 #include "../../include/cilreg_gb300.h"
 #include "drivers.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(NT) k_tv_energy_finish(const double2* __restri
 // energy of device arrays U, U0 into *e_host (synchronous on stream s)
 int tv_energy_run(const float* U, const float* U0, float* e_host, float lambda, int type, const Dims& d,
                   cudaStream_t s) {
+    CILREG_RANGE("cilreg TV energy");
     if (type != 1 && type != 2) return fail(ERR_ARG, __FILE__, __LINE__, "type must be 1 or 2 (got %d)", type);
     if (!e_host) return fail(ERR_ARG, __FILE__, __LINE__, "null E_val");
     const Launch3 L = plan_launch(d);

@@ -15,6 +15,7 @@
 
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
 
 int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int methodTV, int nonneg,
             const Dims& d, cudaStream_t s, float* info, FgpWarm* warm) {
+    CILREG_RANGE("cilreg FGP-TV");
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);

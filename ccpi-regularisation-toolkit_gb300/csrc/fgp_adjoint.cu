@@ -26,6 +26,7 @@
 #include "../../include/cilreg_gb300.h"
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(1024) k_accumulate(const double2* part, long l
 
 int fgp_vjp_run(const float* f, const float* ybar, float lam, int iters, int methodTV, int nonneg, int ckpt,
                 const Dims& d, cudaStream_t s, float* fbar, double* lambar) {
+    CILREG_RANGE("cilreg FGP-TV adjoint");
     if (iters < 1) return fail(ERR_ARG, __FILE__, __LINE__, "the unrolled map needs at least one iteration");
     if (ckpt < 1) ckpt = 1;
     const bool three = d.nz > 1;

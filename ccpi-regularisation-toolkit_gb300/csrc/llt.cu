@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "drivers.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -206,6 +207,7 @@ LltPlan llt_plan(const Dims& d) {
 
 int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
+    CILREG_RANGE("cilreg LLT-ROF");
     Scratch scratch(s);
     const LltPlan T = llt_plan(d);
     IterControl ctl(s, scratch, iters, epsil, T.nblocks);

@@ -11,6 +11,7 @@
 // simple and volumes of 2^31 voxels or more.
 #include "drivers.cuh"
 #include "ndf_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -79,6 +80,7 @@ void launch_ndf(int pen, const Launch3& L, cudaStream_t s, const float* U, float
 
 int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, float tau, int penalty, float epsil,
             const Dims& d, cudaStream_t s, float* info, const float* u_init) {
+    CILREG_RANGE("cilreg NDF");
     const bool linear = (sigma == 0.0f);
     if (!linear && (penalty < 1 || penalty > 5))
         return fail(ERR_ARG, __FILE__, __LINE__, "No penalty function selected! Use 1,2,3,4 or 5.");

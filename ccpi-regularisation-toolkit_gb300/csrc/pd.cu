@@ -9,6 +9,7 @@
 #include "pd_tiled.cuh"
 
 #include <stdlib.h>
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -104,6 +105,7 @@ __global__ void k_pd_select(const StopCtl* ctl, int iter_total, const float* b0,
 
 int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, float lipschitz, int methodTV,
            int nonneg, const Dims& d, cudaStream_t s, float* info) {
+    CILREG_RANGE("cilreg PD-TV");
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);

@@ -8,6 +8,7 @@
 #include "rof_tiled.cuh"
 
 #include <stdlib.h>
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -145,6 +146,7 @@ int rof_launch_step(const float* cur, float* nxt, const float* f, const float* l
 
 int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int iters, float tau, float epsil,
             const Dims& d, cudaStream_t s, float* info, const float* u_init) {
+    CILREG_RANGE("cilreg ROF-TV");
     CILREG_TRY(rof_check_grid(d));
     Scratch scratch(s);
     const long long nparts = rof_partial_slots(d);

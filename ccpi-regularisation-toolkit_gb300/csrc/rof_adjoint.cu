@@ -33,6 +33,7 @@
 
 #include "../../include/cilreg_gb300.h"
 #include "drivers.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -177,6 +178,7 @@ __global__ void k_rof_adj_add(float* __restrict__ dst, const float* __restrict__
 
 int rof_vjp_run(const float* f, const float* ybar, float lam, int iters, float tau, int ckpt, const Dims& d,
                 cudaStream_t s, float* fbar, double* lambar) {
+    CILREG_RANGE("cilreg ROF-TV adjoint");
     if (iters < 1) return fail(ERR_ARG, __FILE__, __LINE__, "the unrolled map needs at least one iteration");
     if (ckpt < 1) return fail(ERR_ARG, __FILE__, __LINE__, "checkpoint interval %d below 1", ckpt);
     if (ckpt > iters) ckpt = iters;

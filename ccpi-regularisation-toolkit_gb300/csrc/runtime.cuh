@@ -10,6 +10,7 @@
 #include <stddef.h>
 
 #include "common.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -207,6 +208,7 @@ int launch_select_pingpong(const StopCtl* ctl, int iter_total, float* const bufs
 
 template <class Enq, class Tail>
 int run_replayed(int iters, int G, cudaStream_t s, Enq enqueue, Tail tail) {
+    CILREG_RANGE("cilreg graph replay");
     const char* env = getenv("CILREG_GRAPH_REPLAY");  // "0": launch every iteration directly (A/B checks)
     const int reps = (G > 0 && (G % 2) == 0 && !(env && env[0] == '0')) ? iters / G : 0;
     // a stream the caller is capturing records the launches as they are

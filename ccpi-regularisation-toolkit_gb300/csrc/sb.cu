@@ -16,6 +16,7 @@
 // The stopping check compares the two sweeps' results (SB_TV_core.c:123-134).
 #include "drivers.cuh"
 #include "sb_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(256) k_sb_shrink(SbArgs a, Dims d, int kz, con
 
 int sb_run(const float* f, float* u_out, float mu, int iters, float epsil, int methodTV, const Dims& d,
            cudaStream_t s, float* info, SbWarm* warm) {
+    CILREG_RANGE("cilreg SB-TV");
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);

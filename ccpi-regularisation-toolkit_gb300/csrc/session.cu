@@ -18,6 +18,7 @@
 
 #include "../../include/cilreg_gb300.h"
 #include "drivers.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 namespace {
@@ -254,12 +255,14 @@ int cilreg_prox_session_create(cilreg_session** out, int alg, const float* param
 
 int cilreg_prox_session_prox(cilreg_session* S, const float* d_in, float* d_out, int iters, float epsil,
                              float* infovector, void* stream) {
+    CILREG_RANGE("cilreg prox");
     if (!S || !d_in || !d_out || d_in == d_out) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
     return session_prox(S, d_in, d_out, iters, epsil, infovector, (cudaStream_t)stream);
 }
 
 int cilreg_prox_session_fista(cilreg_session* S, const float* d_f, float* d_x, int outer, int inner, float step,
                               void* stream) {
+    CILREG_RANGE("cilreg FISTA");
     if (!S || !d_f || !d_x) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
     if (outer < 0 || inner < 0) return fail(ERR_ARG, __FILE__, __LINE__, "negative iteration count");
     cudaStream_t s = (cudaStream_t)stream;
@@ -290,6 +293,7 @@ int cilreg_prox_session_fista(cilreg_session* S, const float* d_f, float* d_x, i
 
 int cilreg_prox_session_admm(cilreg_session* S, const float* d_f, const float* d_w, float* d_x, int outer, int inner,
                              float rho, void* stream) {
+    CILREG_RANGE("cilreg ADMM");
     if (!S || !d_f || !d_x) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
     if (outer < 0 || inner < 0) return fail(ERR_ARG, __FILE__, __LINE__, "negative iteration count");
     if (!(rho > 0.0f)) return fail(ERR_ARG, __FILE__, __LINE__, "rho must be positive");
@@ -316,6 +320,7 @@ int cilreg_prox_session_admm(cilreg_session* S, const float* d_f, const float* d
 
 int cilreg_prox_session_pdhg(cilreg_session* S, const float* d_f, const float* d_w, float* d_x, int outer, int inner,
                              float tau, float sigma, void* stream) {
+    CILREG_RANGE("cilreg PDHG");
     if (!S || !d_f || !d_x) return fail(ERR_ARG, __FILE__, __LINE__, "bad session call");
     if (outer < 0 || inner < 0) return fail(ERR_ARG, __FILE__, __LINE__, "negative iteration count");
     if (!(tau > 0.0f) || !(sigma > 0.0f)) return fail(ERR_ARG, __FILE__, __LINE__, "tau and sigma must be positive");

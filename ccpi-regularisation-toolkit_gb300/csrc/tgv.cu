@@ -14,6 +14,7 @@
 #include "drivers.cuh"
 #include "tgv_batch.cuh"
 #include "tgv_tiled.cuh"
+#include "nvtx.cuh"
 
 namespace cilreg {
 
@@ -411,6 +412,7 @@ int tgv_run_fused(const float* f, float* u_out, float lam, float alpha1, float a
 
 int tgv_run(const float* f, float* u_out, float lam, float alpha1, float alpha0, int iters, float L2, float epsil,
             const Dims& d, cudaStream_t s, float* info) {
+    CILREG_RANGE("cilreg TGV");
     const bool three = d.nz > 1;
     const int np = three ? 3 : 2, nq = three ? 6 : 3;
     Scratch scratch(s);
