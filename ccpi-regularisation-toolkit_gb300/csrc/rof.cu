@@ -157,6 +157,23 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
     float* bufs[2] = {u_out, alt};
     CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
+    const int depth = ctl.checking() ? 0 : rof_tb2d_depth(d, iters);
+    if (depth > 0 && !use_simple_kernel()) {
+        // 2D image, fixed count: `depth` iterations per launch on tiles with
+        // overlapped halos; launches 0 .. nl-2 replayed from a graph, the
+        // last one (the remaining iterations) directly
+        const int nl = (iters + depth - 1) / depth;
+        const int last = iters - (nl - 1) * depth;
+        CILREG_TRY(run_replayed(nl - 1, 16, s, [&](int k, cudaStream_t st, bool) -> int {
+            CILREG_TRY(rof_tb2d_step(bufs[k & 1], bufs[(k + 1) & 1], f, lam_arr, lam, tau, d, depth, st));
+            note_launch();
+            return OK;
+        }));
+        CILREG_TRY(rof_tb2d_step(bufs[(nl - 1) & 1], bufs[nl & 1], f, lam_arr, lam, tau, d, last, s));
+        note_launch();
+        if (nl & 1) CILREG_CUDA(cudaMemcpyAsync(u_out, alt, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+        return ctl.finish(info);
+    }
     if (!ctl.checking() && d.n <= (1LL << 22)) {
         // small volume, fixed count: launch overhead dominates, replay a graph
         CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {

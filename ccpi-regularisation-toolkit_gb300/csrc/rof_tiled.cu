@@ -346,7 +346,145 @@ __global__ void __launch_bounds__(NT, 3) k_rof_async(const float* __restrict__ U
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
+// ---------------------------------------------------------------------------
+// 2D images, fixed iteration counts: `depth` iterations per launch on tiles
+// with overlapped halos (ghost zones).  A CTA loads its 48 x 32 output tile
+// plus `depth` pixels on every side (clipped at the image edge) of U and f
+// (and the lambda map) into shared memory and runs `depth` iterations there:
+// iteration t forms the fluxes on the region less t pixels on each side cut
+// by the halo and updates it less t + 1, so after `depth` iterations the
+// output tile holds U^(k+depth) exactly (a voxel's update reads U only within
+// one pixel of it, diagonals included).  Neighbours outside the valid region
+// are clamped into the region; what they feed lies outside the valid region
+// and is never written out.  The per-pixel arithmetic is that of the 2D path
+// of k_rof_stream.  One launch replaces `depth` launches, and U makes one
+// round trip through L2/DRAM per `depth` iterations.
+constexpr int TBW = 48, TBH = 32;   // output tile
+constexpr int TBMAXD = 8;           // largest depth
+constexpr int TBRW = TBW + 2 * TBMAXD, TBRH = TBH + 2 * TBMAXD;
+constexpr int TBTX = 32, TBTY = 16;
+constexpr int TBARR = TBRW * TBRH;
+
+template <bool LARR>
+__global__ void __launch_bounds__(TBTX * TBTY, 2) k_rof_tb2d(const float* __restrict__ U, float* __restrict__ Un,
+                                                              const float* __restrict__ F,
+                                                              const float* __restrict__ lam_arr, float lam,
+                                                              float tau, Dims d, int depth) {
+    extern __shared__ float smem[];
+    float* sA = smem;
+    float* sB = sA + TBARR;
+    float* sD1 = sB + TBARR;
+    float* sD2 = sD1 + TBARR;
+    float* sF = sD2 + TBARR;
+    float* sL = sF + TBARR;  // lambda map (LARR only)
+    const float EPS = 1.0e-8f;
+    const int nx = d.nx, ny = d.ny;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int ox0 = blockIdx.x * TBW, oy0 = blockIdx.y * TBH;
+    const int rx0 = max(ox0 - depth, 0), ry0 = max(oy0 - depth, 0);
+    const int rx1 = min(ox0 + TBW + depth, nx), ry1 = min(oy0 + TBH + depth, ny);
+    const int rw = rx1 - rx0, rh = ry1 - ry0;
+    const bool cutL = rx0 > 0, cutR = rx1 < nx, cutT = ry0 > 0, cutB = ry1 < ny;
+    // f and the lambda map never change during a run: loaded before waiting
+    // for the previous launch (launch_pdl)
+    for (int y = ty; y < rh; y += TBTY)
+        for (int x = tx; x < rw; x += TBTX) {
+            const int g = (ry0 + y) * nx + rx0 + x;
+            sF[y * TBRW + x] = __ldg(F + g);
+            if (LARR) sL[y * TBRW + x] = __ldg(lam_arr + g);
+        }
+    pdl_wait();
+    pdl_trigger();
+    for (int y = ty; y < rh; y += TBTY)
+        for (int x = tx; x < rw; x += TBTX) sA[y * TBRW + x] = __ldg(U + (ry0 + y) * nx + rx0 + x);
+    __syncthreads();
+    // mirrored neighbours in region coordinates (an axis of length 1 maps to
+    // itself; a neighbour beyond a side cut by the halo is clamped)
+    auto hi_x = [&](int x) { return (nx == 1) ? x : ((rx0 + x + 1 >= nx) ? x - 1 : min(x + 1, rw - 1)); };
+    auto lo_x = [&](int x) { return (nx == 1) ? x : ((rx0 + x - 1 < 0) ? x + 1 : max(x - 1, 0)); };
+    auto hi_y = [&](int y) { return (ny == 1) ? y : ((ry0 + y + 1 >= ny) ? y - 1 : min(y + 1, rh - 1)); };
+    auto lo_y = [&](int y) { return (ny == 1) ? y : ((ry0 + y - 1 < 0) ? y + 1 : max(y - 1, 0)); };
+    float* cur = sA;
+    float* nxt = sB;
+    for (int t = 0; t < depth; t++) {
+        const int fx0 = cutL ? t : 0, fx1 = cutR ? rw - t : rw;
+        const int fy0 = cutT ? t : 0, fy1 = cutB ? rh - t : rh;
+        for (int y = fy0 + ty; y < fy1; y += TBTY) {
+            const int yh = hi_y(y), yl = lo_y(y);
+            for (int x = fx0 + tx; x < fx1; x += TBTX) {
+                const float u = cur[y * TBRW + x];
+                const float xp = cur[y * TBRW + hi_x(x)] - u, xm = u - cur[y * TBRW + lo_x(x)];
+                const float yp = cur[yh * TBRW + x] - u, ym = u - cur[yl * TBRW + x];
+                const float mx2 = minmod_sq(xp, xm), my2 = minmod_sq(yp, ym);
+                sD1[y * TBRW + x] = normalise(yp, yp * yp + mx2 + EPS);
+                sD2[y * TBRW + x] = normalise(xp, xp * xp + my2 + EPS);
+            }
+        }
+        __syncthreads();
+        const int ux0 = cutL ? t + 1 : 0, ux1 = cutR ? rw - t - 1 : rw;
+        const int uy0 = cutT ? t + 1 : 0, uy1 = cutB ? rh - t - 1 : rh;
+        for (int y = uy0 + ty; y < uy1; y += TBTY) {
+            const int yl = lo_y(y);
+            for (int x = ux0 + tx; x < ux1; x += TBTX) {
+                const int o = y * TBRW + x;
+                const float u = cur[o];
+                const float fv = sF[o];
+                const float lv = LARR ? sL[o] : lam;
+                const float div = (sD1[o] - sD1[yl * TBRW + x]) + (sD2[o] - sD2[y * TBRW + lo_x(x)]);
+                nxt[o] = u + tau * (lv * div - (u - fv));
+            }
+        }
+        __syncthreads();
+        float* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    // the output tile (clipped at the image edge)
+    const int ty0 = oy0 - ry0, ty1 = min(oy0 + TBH, ny) - ry0;
+    const int tx0 = ox0 - rx0, tx1 = min(ox0 + TBW, nx) - rx0;
+    for (int y = ty0 + ty; y < ty1; y += TBTY)
+        for (int x = tx0 + tx; x < tx1; x += TBTX) Un[(ry0 + y) * nx + rx0 + x] = cur[y * TBRW + x];
+}
+
+size_t tb2d_smem(bool larr) { return sizeof(float) * TBARR * (larr ? 6 : 5); }
+
+template <bool LARR>
+bool tb2d_smem_ok() {
+    static const bool ok = [] {
+        const bool r = cudaFuncSetAttribute(k_rof_tb2d<LARR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)tb2d_smem(LARR)) == cudaSuccess;
+        cudaGetLastError();
+        return r;
+    }();
+    return ok;
+}
+
 }  // namespace
+
+int rof_tb2d_depth(const Dims& d, int iters) {
+    const char* e = getenv("CILREG_ROF_TB");  // "0": one launch per iteration; a number: the depth
+    if (d.nz != 1 || d.n >= (1LL << 31) || iters < 2) return 0;
+    if (e && e[0] == '0') return 0;
+    int depth = TBMAXD;
+    if (e && atoi(e) > 0) depth = atoi(e) < TBMAXD ? atoi(e) : TBMAXD;
+    return depth;
+}
+
+int rof_tb2d_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
+                  const Dims& d, int depth, cudaStream_t s) {
+    if (depth < 1 || depth > TBMAXD) return fail(ERR_ARG, __FILE__, __LINE__, "depth %d out of range", depth);
+    const bool larr = lam_arr != nullptr;
+    if (!(larr ? tb2d_smem_ok<true>() : tb2d_smem_ok<false>()))
+        return fail(ERR_CUDA, __FILE__, __LINE__, "cannot raise the shared-memory limit of k_rof_tb2d");
+    const dim3 grid((d.nx + TBW - 1) / TBW, (d.ny + TBH - 1) / TBH, 1), block(TBTX, TBTY, 1);
+    if (larr)
+        CILREG_CUDA(launch_pdl(k_rof_tb2d<true>, grid, block, tb2d_smem(true), s, cur, nxt, f, lam_arr, lam, tau, d,
+                               depth));
+    else
+        CILREG_CUDA(launch_pdl(k_rof_tb2d<false>, grid, block, tb2d_smem(false), s, cur, nxt, f, lam_arr, lam, tau,
+                               d, depth));
+    return OK;
+}
 
 RofPlan rof_tiled_plan(const Dims& d) {
     RofPlan T;

@@ -514,3 +514,27 @@ def test_diff4th_streaming_kernel_equals_per_voxel_kernels(shape, monkeypatch):
         assert int(ia[0]) == int(ib[0])
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
+
+
+@pytest.mark.parametrize("shape", [(512, 512), (37, 95), (1, 70), (70, 1), (2, 2), (33, 49), (130, 97)], ids=str)
+@pytest.mark.parametrize("depth", ["8", "3", "1"])
+def test_rof_2d_overlapped_halo_blocks_equal_single_iterations(shape, depth, monkeypatch):
+    """2D ROF-TV at fixed counts runs `depth` iterations per launch on tiles
+    with overlapped halos; the result equals one launch per iteration, for
+    iteration counts that are not multiples of the depth, with a scalar and
+    a per-pixel lambda."""
+    from ccpi.filters.regularisers import ROF_TV
+
+    rng = np.random.default_rng(41 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    lam_map = (0.01 + 0.03 * rng.random(shape)).astype(np.float32)
+    monkeypatch.setenv("CILREG_ROF_TB", depth)
+    for iters in (37, 120):
+        a = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
+        am = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")  # lambda map: the C-OMP ABI, run on the GPU
+        monkeypatch.setenv("CILREG_ROF_TB", "0")
+        b = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
+        bm = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")
+        monkeypatch.setenv("CILREG_ROF_TB", depth)
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(am, bm)
