@@ -11,11 +11,13 @@
 // printing and continuing, and is safe to call from several host threads
 // (each thread gets its own stream; scratch is stream-ordered).
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/mman.h>
 #include <unistd.h>
 
+#include <chrono>
 #include <thread>
 
 #include "../../include/cilreg_gb300.h"
@@ -74,15 +76,37 @@ int host_call(const float* in, float* out, int dev, const Dims& d, bool upload_o
         float* d_out = io.floats(d.n);
         if (!d_in || !d_out) return io.status();
         const size_t bytes = sizeof(float) * (size_t)d.n;
+        // CILREG_HOST_TIMING=1 prints the phases of the call to stderr (diagnostic)
+        const bool timing = getenv("CILREG_HOST_TIMING") != nullptr;
+        const auto t0 = std::chrono::steady_clock::now();
+        auto ms_since = [&](std::chrono::steady_clock::time_point a) {
+            return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+        };
         CILREG_CUDA(cudaMemcpyAsync(d_in, in, bytes, cudaMemcpyHostToDevice, s));
         if (upload_out) CILREG_CUDA(cudaMemcpyAsync(d_out, out, bytes, cudaMemcpyHostToDevice, s));
+        if (timing) CILREG_CUDA(cudaStreamSynchronize(s));
+        const double t_up = timing ? ms_since(t0) : 0.0;
         std::thread pre;
-        if (bytes >= (16u << 20)) pre = std::thread(populate_for_write, (void*)out, bytes);
+        double t_pop = 0.0;
+        if (bytes >= (16u << 20))
+            pre = std::thread([&] {
+                const auto p0 = std::chrono::steady_clock::now();
+                populate_for_write((void*)out, bytes);
+                t_pop = ms_since(p0);
+            });
+        const auto t1 = std::chrono::steady_clock::now();
         rc = body(d_in, d_out, s);
+        if (timing) cudaStreamSynchronize(s);
+        const double t_body = timing ? ms_since(t1) : 0.0;
         if (pre.joinable()) pre.join();
+        const double t_join = timing ? ms_since(t1) - t_body : 0.0;
         if (rc == 0) {
+            const auto t2 = std::chrono::steady_clock::now();
             CILREG_CUDA(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, s));
             CILREG_CUDA(cudaStreamSynchronize(s));
+            if (timing)
+                fprintf(stderr, "cilreg host call: upload %.2f ms, run %.2f ms, populate %.2f ms (waited %.2f), "
+                        "download %.2f ms, total %.2f ms\n", t_up, t_body, t_pop, t_join, ms_since(t2), ms_since(t0));
         }
     }
     return rc;

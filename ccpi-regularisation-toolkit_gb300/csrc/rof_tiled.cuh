@@ -19,8 +19,8 @@ int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* 
                    float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s);
 
 // 2D images, fixed counts: iterations per launch of the overlapped-halo
-// kernel (0 when it does not apply; CILREG_ROF_TB=0 turns it off, a number
-// sets the depth, at most 8)
+// kernel, CILREG_ROF_TB=<depth> (at most 8); 0 (the default) when it is not
+// asked for or does not apply
 int rof_tb2d_depth(const Dims& d, int iters);
 // `depth` iterations in one launch: reads cur, writes nxt (distinct buffers)
 int rof_tb2d_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,

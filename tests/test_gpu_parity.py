@@ -532,7 +532,7 @@ def test_rof_2d_overlapped_halo_blocks_equal_single_iterations(shape, depth, mon
     for iters in (37, 120):
         a = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
         am = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")  # lambda map: the C-OMP ABI, run on the GPU
-        monkeypatch.setenv("CILREG_ROF_TB", "0")
+        monkeypatch.delenv("CILREG_ROF_TB")
         b = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
         bm = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")
         monkeypatch.setenv("CILREG_ROF_TB", depth)
