@@ -92,7 +92,7 @@ def _dev(gpu_device):
 def TV_ROF_GPU(inputData, regularisation_parameter, iterationsNumb, marching_step_parameter, tolerance_param,
                gpu_device, out=None, infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.TV_ROF_GPU_main(ptr(a), ptr(out), ptr(info), float(regularisation_parameter),
                                     int(iterationsNumb), float(marching_step_parameter), float(tolerance_param),
@@ -104,7 +104,7 @@ def TV_ROF_GPU(inputData, regularisation_parameter, iterationsNumb, marching_ste
 def TV_FGP_GPU(inputData, lambdaPar, iterationsNumb, epsil, methodTV, nonneg, gpu_device, out=None,
                infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.TV_FGP_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), int(iterationsNumb),
                                     float(epsil), int(methodTV), int(nonneg), _dev(gpu_device), *dims(a))
@@ -115,7 +115,7 @@ def TV_FGP_GPU(inputData, lambdaPar, iterationsNumb, epsil, methodTV, nonneg, gp
 def PDTV_GPU(Input, lambdaPar, iter, epsil, lipschitz_const, methodTV, nonneg, gpu_device, Output=None,
              infovector=None):
     a = as_input(Input)
-    out = as_output(Output, a)
+    out = as_output(Output, a, zero_init=int(iter) <= 0)
     info = as_info(infovector)
     st = cilregcuda.TV_PD_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), int(iter), float(epsil),
                                    float(lipschitz_const), int(methodTV), int(nonneg), _dev(gpu_device), *dims(a))
@@ -125,7 +125,7 @@ def PDTV_GPU(Input, lambdaPar, iter, epsil, lipschitz_const, methodTV, nonneg, g
 
 def SB_TV_GPU(inputData, lambdaPar, iterationsNumb, epsil, methodTV, gpu_device, out=None, infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.TV_SB_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), int(iterationsNumb),
                                    float(epsil), int(methodTV), _dev(gpu_device), *dims(a))
@@ -138,7 +138,7 @@ def TGV_GPU(inputData, lambdaPar, alpha1, alpha0, iterationsNumb, L2, epsil, gpu
     """TGV on the GPU.  Unlike the reference (TV.py:722-725), the dims are
     passed with dimX fastest, so GPU and CPU results agree for every shape."""
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.TGV_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), float(alpha1), float(alpha0),
                                  int(iterationsNumb), float(L2), float(epsil), _dev(gpu_device), *dims(a))
@@ -187,7 +187,7 @@ def LLT_ROF_CPU(inputData, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil, out
 def LLT_ROF_GPU(inputData, lambdaROF, lambdaLLT, iterationsNumb, tau, epsil, gpu_device, out=None,
                 infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.LLT_ROF_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaROF), float(lambdaLLT),
                                      int(iterationsNumb), float(tau), float(epsil), _dev(gpu_device), *dims(a))
@@ -212,7 +212,7 @@ def dTV_FGP_GPU(inputData, inputRef, lambdaPar, iterationsNumb, epsil, eta, meth
                 out=None, infovector=None):
     a = as_input(inputData)
     r = _as_like(inputRef, a, "inputRef")
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.dTV_FGP_GPU_main(ptr(a), ptr(r), ptr(out), ptr(info), float(lambdaPar), int(iterationsNumb),
                                      float(epsil), float(eta), int(methodTV), int(nonneg), _dev(gpu_device),

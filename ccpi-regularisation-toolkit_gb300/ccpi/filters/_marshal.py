@@ -28,6 +28,10 @@ def as_input(a) -> np.ndarray:
 
 
 def as_output(out, like: np.ndarray, zero_init: bool = True) -> np.ndarray:
+    """The caller's output array, validated, or a new one.  The GPU entry
+    points write their Output whole (they never read it unless they run no
+    iteration), so their wrappers ask for no zero fill: a 512 MiB np.zeros_like
+    costs tens of milliseconds per call."""
     if out is None:
         return np.zeros_like(like) if zero_init else np.empty_like(like)
     if not isinstance(out, np.ndarray) or out.dtype != np.float32:

@@ -39,7 +39,7 @@ def _dev(gpu_device):
 def NDF_GPU(inputData, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype, epsil, gpu_device, out=None,
             infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.NonlDiff_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), float(sigmaPar),
                                       int(iterationsNumb), float(tau), int(penaltytype), float(epsil),
@@ -51,7 +51,7 @@ def NDF_GPU(inputData, lambdaPar, sigmaPar, iterationsNumb, tau, penaltytype, ep
 def Diffus4th_GPU(inputData, lambdaPar, sigmaPar, iterationsNumb, tau, epsil, gpu_device, out=None,
                   infovector=None):
     a = as_input(inputData)
-    out = as_output(out, a)
+    out = as_output(out, a, zero_init=int(iterationsNumb) <= 0)
     info = as_info(infovector)
     st = cilregcuda.Diffus4th_GPU_main(ptr(a), ptr(out), ptr(info), float(lambdaPar), float(sigmaPar),
                                        int(iterationsNumb), float(tau), float(epsil), _dev(gpu_device), *dims(a))
