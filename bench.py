@@ -702,6 +702,42 @@ def configs_bench(args):
     return 0
 
 
+def workload_figures():
+    """Compact figures of the batched (64 uneven volumes, FGP and TGV, 300
+    iterations, device-resident, one graph or persistent launch per
+    regulariser as the autotuner picks) and served (48 prox requests, Poisson
+    mean 200/s) workloads, added to the headline line so that every bench run
+    records them.  The reference per-call legs of --batch / --serve take
+    about a minute more and are left to those modes."""
+    import torch
+    from ccpi.filters.batch import FGP_TV_batch, TGV_batch
+    from ccpi.filters.serving import ProxServer, summarise
+
+    vols = [torch.from_numpy(v).cuda() for v in batch_volumes()]
+    nvox = sum(v.numel() for v in vols)
+    out = {}
+    for name, fn in (("FGP_TV", lambda: FGP_TV_batch(vols, 0.03, 300, 0.0, 0, 1)),
+                     ("TGV", lambda: TGV_batch(vols, 0.03, 1.0, 2.0, 300, 12.0))):
+        fn()  # warm-up (the autotuner times its candidates on the first call of a layout)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        out[name] = {"seconds": dt, "volumes_per_s": len(vols) / dt, "voxel_iters_per_s": nvox * 300 / dt}
+    batched = {"workload": f"{len(vols)} volumes, edges from {{96,...,256}}, {nvox} voxels, 300 iterations",
+               **out}
+    del vols
+    reqs = serve_requests(48)
+    server = ProxServer(slots=8, hbm_budget=150e9)
+    server.serve(reqs[:4], realtime=False)
+    t = time.perf_counter()
+    res = server.serve(reqs)
+    served = summarise(res, time.perf_counter() - t)
+    served["workload"] = "48 prox requests, Poisson mean 200/s, 2D 1024^2 / 3D 128^3-384^3, 5-50 FISTA x 20"
+    return {"batched": batched, "served": served}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -712,6 +748,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=20, help="iterations per reference-arm step")
     ap.add_argument("--cpu-iters", type=int, default=20, help="iterations of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="leave the batched and served figures out of the headline line")
     ap.add_argument("--profile-case", action="store_true",
                     help="only run --steps FGP calls of --iters fixed iterations on the device (for ncu)")
     ap.add_argument("--iters", type=int, default=20, help="iterations per call in --profile-case")
@@ -882,6 +920,10 @@ def main():
         raise RuntimeError("the Python-API call left its output empty or non-finite")
     py_t_max, py_vi_all = reduce_over_ranks(pg, sum(py_times), py_vi, dev)
 
+    workloads = None
+    if rank == 0 and world == 1 and not args.no_workloads:
+        workloads = workload_figures()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, kind, cores, dt = cpu_baseline(x, args.cpu_iters)
@@ -909,6 +951,7 @@ def main():
                                       "host arrays, a new output array per call"},
             "gpu_launches": launches,
             "clocks": clock_info,
+            "workloads": workloads,
         }
         print(json.dumps(line))
     if pg is not None:
