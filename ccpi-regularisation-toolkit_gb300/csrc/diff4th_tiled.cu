@@ -71,13 +71,25 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
     float uj = ld(U, z0);
     float fa = o_pt ? ld(F, z0 - 2) : 0.f, fb = o_pt ? ld(F, z0 - 1) : 0.f;  // f of planes j-2, j-1
 
-    // R = (j - z0) & 3
-    auto step = [&](auto rr, int j) {
+    // the steps whose planes are all inside the volume and the chunk, none of
+    // them the first or last plane of the volume: no plane check, no
+    // mirrored-plane select and no load predicate (halo threads outside the
+    // volume load voxel 0 of the plane, and never use it)
+    const int js0 = max(z0 + 2, 3), js1 = min(z1, nz - 2);  // steady steps: js0 <= j <= js1 (3D)
+    // R = (j - z0) & 3; ST: a steady step
+    auto step = [&](auto rr, auto st, int j) {
         constexpr int R = decltype(rr)::value;
+        constexpr bool ST = THREE && decltype(st)::value;
         constexpr int SJ = R, SM = (R + 3) & 3, SM2 = (R + 2) & 3;  // U slots of planes j, j-1, j-2
         constexpr int WM = (R + 1) & 1, WK = R & 1;                 // W slots of planes j-1, j-2
-        const float un1 = (j + 1 <= z1 + 1) ? ld(U, j + 1) : 0.f;  // prefetch U(j+1)
-        const float fn = o_pt ? ld(F, j) : 0.f;                      // prefetch f(j)
+        float un1, fn;
+        if (ST) {
+            un1 = __ldg(U + ((IT)(j + 1) * sxy + col));  // prefetch U(j+1)
+            fn = __ldg(F + ((IT)j * sxy + col));         // prefetch f(j)
+        } else {
+            un1 = (j + 1 <= z1 + 1) ? ld(U, j + 1) : 0.f;
+            fn = o_pt ? ld(F, j) : 0.f;
+        }
         // B. publish U(j)
         sU[SJ][ty][tx] = uj;
         __syncthreads();
@@ -86,7 +98,7 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
         wc = wb;
         wb = wa;
         wa = 0.f;
-        if (m >= 0 && m < nz && m >= z0 - 1 && m <= z1 && w_pt) {
+        if ((ST || (m >= 0 && m < nz && m >= z0 - 1 && m <= z1)) && w_pt) {
             const float c0 = sU[SM][ty][tx];
             const float um_x = sU[SM][ty][xl], up_x = sU[SM][ty][xh];
             const float um_y = sU[SM][yl][tx], up_y = sU[SM][yh][tx];
@@ -99,8 +111,8 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
             float den, vn, vo;
             if (THREE) {
                 // mirrored k-1 / k+1 planes (an axis of length 1 maps to itself)
-                const float(*pl)[BX] = (nz == 1) ? sU[SM] : ((m == 0) ? sU[SJ] : sU[SM2]);
-                const float(*ph)[BX] = (nz == 1) ? sU[SM] : ((m == nz - 1) ? sU[SM2] : sU[SJ]);
+                const float(*pl)[BX] = ST ? sU[SM2] : ((nz == 1) ? sU[SM] : ((m == 0) ? sU[SJ] : sU[SM2]));
+                const float(*ph)[BX] = ST ? sU[SJ] : ((nz == 1) ? sU[SM] : ((m == nz - 1) ? sU[SM2] : sU[SJ]));
                 const float zm = pl[ty][tx], zp = ph[ty][tx];
                 const float gz = 0.5f * (zm - zp);
                 const float gz2 = gz * gz;
@@ -130,14 +142,14 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
         // C. update plane kf = j-2 (Diffus4th_order_core.c:237-265); its W was
         // published in the previous step
         const int kf = j - 2;
-        if (o_pt && kf >= z0 && kf < z1) {
+        if (o_pt && (ST || (kf >= z0 && kf < z1))) {
             const float w = sW[WK][ty][tx];
             const float lx = sW[WK][ty][xl] + sW[WK][ty][xh] - 2.0f * w;
             const float ly = sW[WK][yl][tx] + sW[WK][yh][tx] - 2.0f * w;
             float lap = lx + ly;
             if (THREE) {
-                const float wlo = (nz == 1) ? w : ((kf == 0) ? wa : wc);        // mirrored W(k-1)
-                const float whi = (nz == 1) ? w : ((kf == nz - 1) ? wc : wa);   // mirrored W(k+1)
+                const float wlo = ST ? wc : ((nz == 1) ? w : ((kf == 0) ? wa : wc));       // mirrored W(k-1)
+                const float whi = ST ? wa : ((nz == 1) ? w : ((kf == nz - 1) ? wc : wa));  // mirrored W(k+1)
                 lap = lap + (wlo + whi - 2.0f * w);
             }
             const float u = sU[SM2][ty][tx];
@@ -153,16 +165,22 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
         fa = fb;
         fb = fn;
     };
+    // each position of the unrolled loop runs the steady or the general step
+    // (a branch on the plane index, the same for the whole CTA)
+    auto any = [&](auto rr, int jj) {
+        if (jj >= js0 && jj <= js1) step(rr, std::true_type{}, jj);
+        else step(rr, std::false_type{}, jj);
+    };
     int j = z0;
     for (; j + 3 <= z1 + 1; j += 4) {
-        step(Ic<0>{}, j);
-        step(Ic<1>{}, j + 1);
-        step(Ic<2>{}, j + 2);
-        step(Ic<3>{}, j + 3);
+        any(Ic<0>{}, j);
+        any(Ic<1>{}, j + 1);
+        any(Ic<2>{}, j + 2);
+        any(Ic<3>{}, j + 3);
     }
-    if (j <= z1 + 1) step(Ic<0>{}, j);
-    if (j + 1 <= z1 + 1) step(Ic<1>{}, j + 1);
-    if (j + 2 <= z1 + 1) step(Ic<2>{}, j + 2);
+    if (j <= z1 + 1) step(Ic<0>{}, std::false_type{}, j);
+    if (j + 1 <= z1 + 1) step(Ic<1>{}, std::false_type{}, j + 1);
+    if (j + 2 <= z1 + 1) step(Ic<2>{}, std::false_type{}, j + 2);
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
