@@ -95,12 +95,17 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
     float uj = __ldg(U + at(z0));
     float fa = o_pt ? __ldg(F + at(z0 - 2)) : 0.f, fb = o_pt ? __ldg(F + at(z0 - 1)) : 0.f;
 
-    auto step = [&](auto rr, int j) {
+    // steady steps (js0 <= j <= js1, 3D): every plane inside the volume and
+    // the chunk and none the first or last plane of the volume, so no clamp,
+    // no mirrored-plane select and no range test
+    const int js0 = max(z0 + 2, 3), js1 = min(z1 + 1, nz - 2);
+    auto step = [&](auto rr, auto st, int j) {
         constexpr int R = decltype(rr)::value;
+        constexpr bool ST = THREE && decltype(st)::value;
         constexpr int SJ = R, SM = (R + 3) & 3, SM2 = (R + 2) & 3;  // U slots of planes j, j-1, j-2
         constexpr int WM = (R + 1) & 1, WK = R & 1;                 // flux slots of planes j-1, j-2
-        const float un1 = __ldg(U + at(j + 1));                    // prefetch U(j+1)
-        const float fn = o_pt ? __ldg(F + at(j)) : 0.f;              // prefetch f(j)
+        const float un1 = __ldg(U + (ST ? (IT)(j + 1) * sxy + col : at(j + 1)));  // prefetch U(j+1)
+        const float fn = o_pt ? __ldg(F + (ST ? (IT)j * sxy + col : at(j))) : 0.f;  // prefetch f(j)
         // B. publish U(j)
         sU[SJ][oc] = uj;
         __syncthreads();
@@ -108,8 +113,8 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
         const int m = j - 1;
         {
             const float* Um = sU[SM];
-            const float* Ulo = THREE ? ((m == 0) ? sU[SJ] : sU[SM2]) : Um;
-            const float* Uhi = THREE ? ((m == nz - 1) ? sU[SM2] : sU[SJ]) : Um;
+            const float* Ulo = ST ? sU[SM2] : (THREE ? ((m == 0) ? sU[SJ] : sU[SM2]) : Um);
+            const float* Uhi = ST ? sU[SJ] : (THREE ? ((m == nz - 1) ? sU[SM2] : sU[SJ]) : Um);
             const float c = Um[oc];
             const float xp = Um[oxh] - c, xm = c - Um[oxl];
             const float yp = Um[oyh] - c, ym = c - Um[oyl];
@@ -138,7 +143,7 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
         }
         // C. update plane kf = j-2 (its terms were published in the previous step)
         const int kf = j - 2;
-        if (o_pt && kf >= z0 && kf < z1) {
+        if (o_pt && (ST || (kf >= z0 && kf < z1))) {
             const float w1 = sL1[WK][oc], w2 = sL2[WK][oc];
             const float dxx = sL1[WK][oxh] - 2.0f * w1 + sL1[WK][oxl];
             const float dyy = sL2[WK][oyh] - 2.0f * w2 + sL2[WK][oyl];
@@ -146,11 +151,11 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
             const float dv2 = sR2[WK][oc] - sR2[WK][oxl];
             float laplc, div;
             if (THREE) {
-                const float llo = (kf == 0) ? l3a : l3c;        // mirrored k-1
-                const float lhi = (kf == nz - 1) ? l3c : l3a;   // mirrored k+1
+                const float llo = (!ST && kf == 0) ? l3a : l3c;        // mirrored k-1
+                const float lhi = (!ST && kf == nz - 1) ? l3c : l3a;   // mirrored k+1
                 const float dzz = lhi - 2.0f * l3b + llo;
                 laplc = dxx + dyy + dzz;
-                const float rlo = (kf == 0) ? r3a : r3c;
+                const float rlo = (!ST && kf == 0) ? r3a : r3c;
                 div = dv1 + dv2 + (r3b - rlo);
             } else {
                 laplc = dxx + dyy;
@@ -169,16 +174,22 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
         fa = fb;
         fb = fn;
     };
+    // each position of the unrolled loop runs the steady or the general step
+    // (a branch on the plane index, the same for the whole CTA)
+    auto any = [&](auto rr, int jj) {
+        if (jj >= js0 && jj <= js1) step(rr, std::true_type{}, jj);
+        else step(rr, std::false_type{}, jj);
+    };
     int j = z0;
     for (; j + 3 <= z1 + 1; j += 4) {
-        step(Ic<0>{}, j);
-        step(Ic<1>{}, j + 1);
-        step(Ic<2>{}, j + 2);
-        step(Ic<3>{}, j + 3);
+        any(Ic<0>{}, j);
+        any(Ic<1>{}, j + 1);
+        any(Ic<2>{}, j + 2);
+        any(Ic<3>{}, j + 3);
     }
-    if (j <= z1 + 1) step(Ic<0>{}, j);
-    if (j + 1 <= z1 + 1) step(Ic<1>{}, j + 1);
-    if (j + 2 <= z1 + 1) step(Ic<2>{}, j + 2);
+    if (j <= z1 + 1) step(Ic<0>{}, std::false_type{}, j);
+    if (j + 1 <= z1 + 1) step(Ic<1>{}, std::false_type{}, j + 1);
+    if (j + 2 <= z1 + 1) step(Ic<2>{}, std::false_type{}, j + 2);
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
