@@ -488,6 +488,7 @@ int rof_tb2d_step(const float* cur, float* nxt, const float* f, const float* lam
 }
 
 RofPlan rof_tiled_plan(const Dims& d) {
+    if (rof_pair_applies(d)) return rof_pair_plan(d);
     RofPlan T;
     T.block = dim3(BX, BY, 1);
     const long long tiles = (long long)((d.nx + OX - 1) / OX) * ((d.ny + OY - 1) / OY);
@@ -505,6 +506,7 @@ RofPlan rof_tiled_plan(const Dims& d) {
 
 int rof_tiled_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,
                    float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
+    if (T.pair) return rof_pair_step(T, cur, nxt, f, lam_arr, lam, tau, d, ctl, check, partials, s);
     const bool three = d.nz > 1, larr = lam_arr != nullptr;
     const char* ek = getenv("CILREG_ROF_KERNEL");
     if (three && d.n < (1LL << 31) && !(ek && ek[0] == 'r')) {

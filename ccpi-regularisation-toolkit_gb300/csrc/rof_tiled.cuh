@@ -9,9 +9,17 @@ struct RofPlan {
     dim3 grid, block;
     long long nblocks = 0;
     int zchunk = 0;
+    bool pair = false;  // the two-voxels-per-thread kernel (rof_pair.cu)
 };
 
 RofPlan rof_tiled_plan(const Dims& d);
+
+// 3D volumes with nx even and fewer than 2^31 voxels run k_rof_pair
+// (CILREG_ROF_KERNEL=async, reg or simple select a one-voxel kernel)
+bool rof_pair_applies(const Dims& d);
+RofPlan rof_pair_plan(const Dims& d);
+int rof_pair_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,
+                  float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s);
 
 // one iteration: reads cur, writes nxt; on a check iteration one FP64 partial
 // per CTA (RofPlan::nblocks of them)

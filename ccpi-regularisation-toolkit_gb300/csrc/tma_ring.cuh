@@ -70,6 +70,10 @@ __device__ __forceinline__ bool wait_stage(uint64_t* bar, int use) {
 __device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(sdst)), "l"(gsrc) : "memory");
 }
+// ... of 8 bytes (both addresses 8-byte aligned)
+__device__ __forceinline__ void cp_async8(float* sdst, const float* gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(sdst)), "l"(gsrc) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {

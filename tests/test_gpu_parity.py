@@ -375,9 +375,12 @@ def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
-                                   (130, 33, 35), (151, 12, 31)], ids=str)
+                                   (130, 33, 35), (151, 12, 31), (67, 70, 10), (130, 33, 64), (5, 31, 62),
+                                   (3, 47, 2), (9, 61, 124), (4, 2, 90)], ids=str)
 def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
-    """The 2.5D streaming ROF kernel and the per-voxel kernel compute the same iteration."""
+    """The 2.5D streaming ROF kernels and the per-voxel kernel compute the same
+    iteration (3D volumes with an even row length run the two-voxel kernel by
+    default; odd rows and the tile edges at 30 n - 1 and 30 n + 28 included)."""
     from ccpi.filters.regularisers import ROF_TV
 
     rng = np.random.default_rng(11 + sum(shape))
@@ -386,8 +389,9 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         ib = np.zeros(2, np.float32)
         monkeypatch.setenv("CILREG_ROF_KERNEL", "simple")
         b = ROF_TV(x, 0.02, 120, 0.001, epsil, device="gpu", infovector=ib)
-        # default (3D: asynchronous-copy staging) and the register-pipelined kernel
-        for kernel in (None, "reg"):
+        # default, the one-voxel kernel with asynchronous-copy staging and the
+        # register-pipelined kernel
+        for kernel in (None, "async", "reg"):
             if kernel is None:
                 monkeypatch.delenv("CILREG_ROF_KERNEL")
             else:
@@ -459,7 +463,7 @@ def test_tgv_streaming_kernels_equal_per_voxel_kernels(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
-@pytest.mark.parametrize("shape", [(48, 61), (10, 16, 22), (70, 33, 35)], ids=str)
+@pytest.mark.parametrize("shape", [(48, 61), (10, 16, 22), (70, 33, 35), (20, 33, 46)], ids=str)
 def test_rof_per_voxel_lambda_matches_oracle(shape, monkeypatch):
     """ROF with a per-voxel lambda map (ROF_TV_core.c:280 lambda_is_arr) through the
     C-OMP entry point, against the oracle, on both GPU kernels."""
@@ -538,3 +542,50 @@ def test_rof_2d_overlapped_halo_blocks_equal_single_iterations(shape, depth, mon
         monkeypatch.setenv("CILREG_ROF_TB", depth)
         np.testing.assert_array_equal(a, b)
         np.testing.assert_array_equal(am, bm)
+
+
+@pytest.mark.parametrize("lam_map", [False, True], ids=["scalar_lambda", "lambda_map"])
+def test_rof_pair_kernel_with_arrays_off_8_byte_alignment(lam_map):
+    """The two-voxel ROF kernel reads and writes voxel pairs with 8-byte
+    accesses; arrays that start 4 bytes off an 8-byte boundary (device
+    pointers into the middle of a buffer) run its 4-byte variant, which must
+    give the same iterates bit for bit."""
+    import ctypes
+    import os
+
+    import torch
+    from conftest import PKG
+
+    P = ctypes.POINTER(ctypes.c_float)
+    lib = ctypes.CDLL(os.path.join(PKG, "ccpi", "filters", "libcilregcuda.so"))
+    lib.cilreg_rof_tv_dev.argtypes = [ctypes.c_void_p, ctypes.c_void_p, P, ctypes.c_void_p, ctypes.c_float,
+                                      ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_void_p]
+    lib.cilreg_rof_tv_dev.restype = ctypes.c_int
+    lib.cilreg_last_error.restype = ctypes.c_char_p
+    shape = (37, 45, 66)
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(41)
+    x = rng.random(shape).astype(np.float32)
+    lm = (0.01 + 0.03 * rng.random(shape)).astype(np.float32)
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for off in (0, 1):
+        buf_in = torch.zeros(n + 2, device="cuda")
+        buf_out = torch.zeros(n + 2, device="cuda")
+        buf_lam = torch.zeros(n + 2, device="cuda")
+        buf_in[off:off + n] = torch.from_numpy(x.ravel()).cuda()
+        buf_lam[off:off + n] = torch.from_numpy(lm.ravel()).cuda()
+        info = np.zeros(2, np.float32)
+        st = lib.cilreg_rof_tv_dev(buf_in.data_ptr() + 4 * off, buf_out.data_ptr() + 4 * off,
+                                   info.ctypes.data_as(P), buf_lam.data_ptr() + 4 * off if lam_map else None,
+                                   0.02, 90, 0.001, 1e-4, shape[2], shape[1], shape[0], stream)
+        assert st == 0, lib.cilreg_last_error()
+        torch.cuda.synchronize()
+        outs.append((buf_out[off:off + n].cpu().numpy().reshape(shape), info.copy()))
+    (a, ia), (b, ib) = outs
+    assert int(ia[0]) == int(ib[0])
+    np.testing.assert_array_equal(a, b)
+    # the oracle at the iteration count the stopping rule gave
+    ref, _ = O.rof_tv(x, lm if lam_map else 0.02, int(ia[0]), 0.001, 0.0)
+    assert np.max(np.abs(a - ref)) <= rel_tol(ref, 1e-5)
