@@ -6,9 +6,10 @@
 // result depends on the thread count).  Here every sweep reads the previous
 // iterate only (ping-pong buffers): deterministic, and equal to the
 // reference run with one thread up to the update order.  One kernel per
-// iteration: the 2.5D streaming kernel of ndf_tiled.cu (12 B of HBM traffic
-// per voxel-iteration), or the per-voxel kernel below for CILREG_NDF_KERNEL=
-// simple and volumes of 2^31 voxels or more.
+// iteration: a 2.5D streaming kernel (12 B of HBM traffic per
+// voxel-iteration; two voxels per thread in ndf_pair.cu for 3D volumes with
+// an even row length, one in ndf_tiled.cu otherwise), or the per-voxel kernel
+// below for CILREG_NDF_KERNEL=simple and volumes of 2^31 voxels or more.
 #include "drivers.cuh"
 #include "ndf_tiled.cuh"
 #include "nvtx.cuh"

@@ -21,6 +21,8 @@
 //      summed in the reference's order.
 // One barrier per plane, no boundary branches in the loop, ring slots as
 // compile-time constants.  HBM traffic: read U and f, write U (12 B/voxel).
+#include <string.h>
+
 #include <type_traits>
 
 #include "ndf_tiled.cuh"
@@ -181,11 +183,12 @@ cudaError_t launch(int pen, const NdfPlan& T, cudaStream_t s, const float* cur, 
 }  // namespace
 
 NdfPlan ndf_stream_plan(const Dims& d) {
+    if (ndf_pair_applies(d)) return ndf_pair_plan(d);
     NdfPlan T;
     const char* e = getenv("CILREG_NDF_KERNEL");
     // "simple" selects the per-voxel kernel; volumes of 2^31 voxels or more use
     // it too (the streaming kernel indexes with 32-bit offsets)
-    T.use = !(e && e[0] == 's') && d.n < (1LL << 31);
+    T.use = !(e && strcmp(e, "simple") == 0) && d.n < (1LL << 31);
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
         static const int resident = resident_ctas(k_ndf_stream<true, 1, false>, NT);
@@ -202,6 +205,7 @@ NdfPlan ndf_stream_plan(const Dims& d) {
 int ndf_stream_step(const NdfPlan& T, int pen, const float* cur, float* nxt, const float* f, float lam, float sg,
                     float isg, float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials,
                     cudaStream_t s) {
+    if (T.pair) return ndf_pair_step(T, pen, cur, nxt, f, lam, sg, isg, tau, d, ctl, check, partials, s);
     if (d.nz > 1) {
         if (check)
             CILREG_CUDA((launch<true, true>(pen, T, s, cur, nxt, f, lam, sg, isg, tau, d, ctl, partials)));

@@ -40,10 +40,19 @@ struct NdfPlan {
     dim3 grid, block;
     long long nblocks = 0;
     int zchunk = 0;
-    bool use = false;  // false: the per-voxel kernel of ndf.cu runs instead
+    bool use = false;   // false: the per-voxel kernel of ndf.cu runs instead
+    bool pair = false;  // the two-voxels-per-thread kernel (ndf_pair.cu)
 };
 
+// the plan of the kernel that runs for `d`: 3D volumes with nx even and
+// fewer than 2^31 voxels run k_ndf_pair, other volumes below 2^31 voxels
+// k_ndf_stream (CILREG_NDF_KERNEL=stream or simple select a one-voxel kernel)
 NdfPlan ndf_stream_plan(const Dims& d);
+bool ndf_pair_applies(const Dims& d);
+NdfPlan ndf_pair_plan(const Dims& d);
+int ndf_pair_step(const NdfPlan& T, int pen, const float* cur, float* nxt, const float* f, float lam, float sg,
+                  float isg, float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials,
+                  cudaStream_t s);
 int ndf_stream_step(const NdfPlan& T, int pen, const float* cur, float* nxt, const float* f, float lam, float sg,
                     float isg, float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials,
                     cudaStream_t s);

@@ -30,6 +30,7 @@
 #include <type_traits>
 
 #include "rof_tiled.cuh"
+#include "pair.cuh"
 #include "tma_ring.cuh"
 
 namespace cilreg {
@@ -41,9 +42,8 @@ using tma::cp_async8;
 using tma::cp_async_commit;
 using tma::cp_async_wait;
 
-constexpr int PX = 16;      // threads along x, one voxel pair each
-constexpr int TW = 2 * PX;  // tile points along x
-constexpr int OXP = TW - 2;
+using namespace pair;
+
 constexpr int AHEAD = 4, RING = 8;
 constexpr int ZCHUNK = 64;
 
@@ -54,20 +54,6 @@ struct Geo {
     static constexpr int MINB = 64 / ROWS;  // CTAs per SM at 64 registers
     static constexpr size_t SMEM = sizeof(float) * TP * (RING + 4);  // U ring, D1 and D2 (two planes each)
 };
-
-template <int V>
-using Ic = std::integral_constant<int, V>;
-template <int V>
-__device__ __forceinline__ constexpr int ival(Ic<V>) {
-    return V;
-}
-__device__ __forceinline__ int ival(int v) { return v; }
-
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 // square of minmod(a, b) per component (ROF_TV_core.c:132): the median of a,
 // b and 0 has its magnitude
@@ -82,8 +68,8 @@ __device__ __forceinline__ float2 normalise2(float2 dp, float2 s) {
     return mul2(dp, make_float2(rsqrtf(s.x), rsqrtf(s.y)));
 }
 
-__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
-__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
 
 template <bool CHECK, bool LARR, bool ALIGNED, int ROWS>
 __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
@@ -102,7 +88,7 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
     const float2 tau2 = splat(tau);
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int X = blockIdx.x * OXP - 2 + 2 * tx;  // x of the pair's first voxel
+    const int X = tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first voxel
     const int y = blockIdx.y * OYP - 1 + ty;
     const bool row_upd = ty >= 1 && ty <= TH - 2 && y >= 0 && y < ny;
     const bool vx = row_upd && tx >= 1 && X >= 0 && X < nx;           // first voxel updated
@@ -125,18 +111,10 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, nz);
     const int sxy = d.sxy;
-    // ring planes beyond the volume hold its mirrored planes (plane -1 holds
-    // plane 1, plane nz holds plane nz-2), so that the k neighbours of the
-    // first and last plane need no select (ROF_TV_core.c:117-118); planes
-    // further out are clamped into the volume and feed no update
-    auto ring_plane = [&](int k) -> int {
-        k = (k < 0) ? -k : k;
-        return (k < nz) ? k : max(2 * nz - 2 - k, 0);
-    };
     auto slot_of = [&](int r) -> float* { return ring + (r & (RING - 1)) * TP; };
     auto issue = [&](int r, int k) {
         float* dst = slot_of(r) + o;
-        const float* src = U + (min(ring_plane(k), nz - 1) * sxy + col);
+        const float* src = U + (ring_plane(k, nz) * sxy + col);
         if (ALIGNED) {
             cp_async8(dst, src);
         } else {
@@ -170,19 +148,19 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
         const float* Uj = slot_of(r + 2);
         const float* Um = slot_of(r + 1);
         const float* Ua = slot_of(r);
-        const float2 ub = lds2(Um + o), uc = lds2(Uj + o), ua = lds2(Ua + o);
+        const float2 ub = ld2(Um + o), uc = ld2(Uj + o), ua = ld2(Ua + o);
         // A. fluxes of plane j-1 (its k neighbours ua, uc already mirrored)
         const float dxc = ub.y - ub.x;  // x+1 minus x: forward difference of the first voxel, backward of the second
         const float2 xp = make_float2(dxc, Um[oxh] - ub.y);
         const float2 xm = make_float2(ub.x - Um[oxl], dxc);
-        const float2 yp = sub2(lds2(Um + oyh), ub), ym = sub2(ub, lds2(Um + oyl));
+        const float2 yp = sub2(ld2(Um + oyh), ub), ym = sub2(ub, ld2(Um + oyl));
         const float2 zp = sub2(uc, ub), zm = sub2(ub, ua);
         const float2 mx2 = minmod_sq2(xp, xm), my2 = minmod_sq2(yp, ym), mz2 = minmod_sq2(zp, zm);
         const float2 n1 = normalise2(yp, add2(add2(fma2(yp, yp, mx2), mz2), EPS2));
         const float2 n2 = normalise2(xp, add2(add2(fma2(xp, xp, my2), mz2), EPS2));
         const float2 n3 = normalise2(zp, add2(add2(fma2(zp, zp, my2), mx2), EPS2));
-        sts2(sD1 + (1 - P) * TP + o, n1);
-        sts2(sD2 + (1 - P) * TP + o, n2);
+        st2(sD1 + (1 - P) * TP + o, n1);
+        st2(sD2 + (1 - P) * TP + o, n2);
         // C. update plane j-2 (ROF_TV_core.c:269-297): lower fluxes D1(i-1)
         // from the row below, D2(j-1) of the first voxel from the left
         // neighbour and of the second from the first, D3 of plane j-3
@@ -190,22 +168,12 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
         if (FULL) {
             const int kf = j - 2;
             const float2 d3lo = (FIRST && kf == 0) ? n3 : d3oo;
-            const float2 d1l = lds2(sD1 + P * TP + oyl);
+            const float2 d1l = ld2(sD1 + P * TP + oyl);
             const float2 d2l = make_float2(sD2[P * TP + oxl], d2o.x);
             const float2 div = add2(add2(sub2(d1o, d1l), sub2(d2o, d2l)), sub2(d3o, d3lo));
             const float2 t = sub2(ua, fa);
             const float2 un = fma2(tau2, fma2(la, div, make_float2(-t.x, -t.y)), ua);
-            float* dst = Un + (kf * sxy + col);
-            if (ALIGNED) {
-                // one 8-byte store where both voxels are updated, one 4-byte
-                // store at the tile and volume edges (predicated, no branch)
-                if (vx && vy) sts2(dst, un);
-                if (vx && !vy) dst[0] = un.x;
-                if (vy && !vx) dst[1] = un.y;
-            } else {
-                if (vx) dst[0] = un.x;
-                if (vy) dst[1] = un.y;
-            }
+            store_pair<ALIGNED>(Un + (kf * sxy + col), un, vx, vy);
             if (CHECK) {
                 const float2 df = sub2(un, ua);
                 const float2 dm = make_float2(vx ? df.x : 0.f, vy ? df.y : 0.f);
@@ -273,8 +241,6 @@ bool smem_ready() {
     return ok;
 }
 
-bool aligned8(const void* p) { return ((uintptr_t)p & 7) == 0; }
-
 }  // namespace
 
 bool rof_pair_applies(const Dims& d) {
@@ -287,7 +253,7 @@ RofPlan rof_pair_plan(const Dims& d) {
     RofPlan T;
     T.pair = true;
     T.block = dim3(PX, ROWS, 1);
-    const int gx = (d.nx + OXP) / OXP, gy = (d.ny + Geo<ROWS>::OYP - 1) / Geo<ROWS>::OYP;
+    const int gx = tiles_x(d.nx), gy = (d.ny + Geo<ROWS>::OYP - 1) / Geo<ROWS>::OYP;
     int resident = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &resident, k_rof_pair<false, false, true, ROWS>, Geo<ROWS>::NTP, Geo<ROWS>::SMEM);
@@ -302,7 +268,8 @@ RofPlan rof_pair_plan(const Dims& d) {
 int rof_pair_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,
                   float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
     const bool larr = lam_arr != nullptr;
-    const bool aligned = aligned8(cur) && aligned8(nxt) && aligned8(f) && (!larr || aligned8(lam_arr));
+    const bool aligned =
+        host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f) && (!larr || host_aligned8(lam_arr));
     if (!smem_ready())
         return fail(ERR_CUDA, __FILE__, __LINE__, "cannot raise the shared-memory limit of k_rof_pair");
     CILREG_CUDA(launch_pdl(pick(check != 0, larr, aligned), T.grid, T.block, Geo<ROWS>::SMEM, s, cur, nxt, f,

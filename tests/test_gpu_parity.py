@@ -404,11 +404,14 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
-                                   (130, 33, 35)], ids=str)
+                                   (130, 33, 35), (67, 70, 10), (5, 31, 62), (3, 47, 2), (9, 1, 124), (4, 2, 90)],
+                         ids=str)
 @pytest.mark.parametrize("penalty", [0, 1, 2, 3, 4, 5])
 def test_ndf_streaming_kernel_equals_per_voxel_kernel(shape, penalty, monkeypatch):
-    """The 2.5D streaming NDF kernel (one flux per face, used with both signs) and
-    the per-voxel kernel (six fluxes per voxel) compute the same iteration."""
+    """The 2.5D streaming NDF kernels (one flux per face, used with both signs;
+    3D volumes with an even row length run the two-voxel kernel by default)
+    and the per-voxel kernel (six fluxes per voxel) compute the same
+    iteration."""
     from ccpi.filters.regularisers import NDF
 
     rng = np.random.default_rng(17 + sum(shape) + penalty)
@@ -416,13 +419,19 @@ def test_ndf_streaming_kernel_equals_per_voxel_kernel(shape, penalty, monkeypatc
     sigma = 0.0 if penalty == 0 else 0.08
     pen = 1 if penalty == 0 else penalty
     for epsil in (0.0, 1e-3):
-        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
-        a = NDF(x, 0.03, sigma, 90, 0.01, pen, epsil, device="gpu", infovector=ia)
+        ib = np.zeros(2, np.float32)
         monkeypatch.setenv("CILREG_NDF_KERNEL", "simple")
         b = NDF(x, 0.03, sigma, 90, 0.01, pen, epsil, device="gpu", infovector=ib)
+        for kernel in (None, "stream"):
+            if kernel is None:
+                monkeypatch.delenv("CILREG_NDF_KERNEL")
+            else:
+                monkeypatch.setenv("CILREG_NDF_KERNEL", kernel)
+            ia = np.zeros(2, np.float32)
+            a = NDF(x, 0.03, sigma, 90, 0.01, pen, epsil, device="gpu", infovector=ia)
+            assert int(ia[0]) == int(ib[0])
+            assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
         monkeypatch.delenv("CILREG_NDF_KERNEL")
-        assert int(ia[0]) == int(ib[0])
-        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
