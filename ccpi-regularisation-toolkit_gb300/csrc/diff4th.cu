@@ -5,6 +5,8 @@
 // in 3D), then U += tau (-lambda Lap(W) - (U - f)) in place (each voxel
 // reads W at its mirrored neighbours and U, f at itself only).
 #include "diff4th_tiled.cuh"
+#include <string.h>
+
 #include "drivers.cuh"
 
 #include <stdlib.h>
@@ -117,7 +119,7 @@ int diff4th_run(const float* f, float* u_out, float lam, float sigma, int iters,
     const Launch3 L = plan_launch(d);
     // CILREG_D4_KERNEL=simple selects the two per-voxel kernels (kept for A/B checks)
     const char* ek = getenv("CILREG_D4_KERNEL");
-    const bool stream = !(ek && ek[0] == 's');
+    const bool stream = !(ek && strcmp(ek, "simple") == 0);
     const D4Plan T = d4_stream_plan(d);
     IterControl ctl(s, scratch, iters, epsil, stream ? T.nblocks : num_blocks(L));
     CILREG_TRY(ctl.status());

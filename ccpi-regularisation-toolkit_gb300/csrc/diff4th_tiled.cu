@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(NT, 2) k_d4_stream(const float* __restrict__ U
 }  // namespace
 
 D4Plan d4_stream_plan(const Dims& d) {
+    if (d4_pair_applies(d)) return d4_pair_plan(d);
     D4Plan T;
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
@@ -203,6 +204,7 @@ D4Plan d4_stream_plan(const Dims& d) {
 
 int d4_stream_step(const D4Plan& T, const float* cur, float* nxt, const float* f, float lam, float tau, float isg2,
                    const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
+    if (T.pair) return d4_pair_step(T, cur, nxt, f, lam, tau, isg2, d, ctl, check, partials, s);
     const bool three = d.nz > 1;
     decltype(&k_d4_stream<true, true, int>) kern;
     if (d.n < (1LL << 31))

@@ -510,22 +510,31 @@ def test_pd_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
-@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35),
+                                   (67, 70, 10), (5, 31, 62), (3, 47, 2), (9, 1, 124), (4, 2, 90), (70, 29, 56)],
                          ids=str)
 def test_diff4th_streaming_kernel_equals_per_voxel_kernels(shape, monkeypatch):
-    """The 2.5D streaming Diff4th kernel and the two per-voxel kernels compute the same iteration."""
+    """The 2.5D streaming Diff4th kernels (3D volumes with an even row length
+    run the two-voxel kernel by default) and the two per-voxel kernels compute
+    the same iteration."""
     from ccpi.filters.regularisers import Diff4th
 
     rng = np.random.default_rng(17 + sum(shape))
     x = rng.random(shape).astype(np.float32)
     for epsil in (0.0, 1e-3):
-        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
-        a = Diff4th(x, 0.8, 0.02, 60, 1e-4, epsil, device="gpu", infovector=ia)
+        ib = np.zeros(2, np.float32)
         monkeypatch.setenv("CILREG_D4_KERNEL", "simple")
         b = Diff4th(x, 0.8, 0.02, 60, 1e-4, epsil, device="gpu", infovector=ib)
+        for kernel in (None, "stream"):
+            if kernel is None:
+                monkeypatch.delenv("CILREG_D4_KERNEL")
+            else:
+                monkeypatch.setenv("CILREG_D4_KERNEL", kernel)
+            ia = np.zeros(2, np.float32)
+            a = Diff4th(x, 0.8, 0.02, 60, 1e-4, epsil, device="gpu", infovector=ia)
+            assert int(ia[0]) == int(ib[0])
+            assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
         monkeypatch.delenv("CILREG_D4_KERNEL")
-        assert int(ia[0]) == int(ib[0])
-        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
 
