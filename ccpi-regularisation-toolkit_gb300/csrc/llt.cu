@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "drivers.cuh"
+#include "llt.cuh"
 #include "nvtx.cuh"
 
 namespace cilreg {
@@ -193,13 +194,8 @@ __global__ void __launch_bounds__(NT, 2) k_llt_stream(const float* __restrict__ 
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
-struct LltPlan {
-    dim3 grid, block;
-    long long nblocks = 0;
-    int zchunk = 0;
-};
-
 LltPlan llt_plan(const Dims& d) {
+    if (llt_pair_applies(d)) return llt_pair_plan(d);
     LltPlan T;
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
@@ -228,20 +224,9 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
     float* bufs[2] = {u_out, alt};
     CILREG_CUDA(cudaMemcpyAsync(u_out, f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     const bool three = d.nz > 1;
-    int it = 0;
-    if (!ctl.checking() && d.n <= (1LL << 22)) {
-        // small volume, fixed count: launch overhead dominates, replay a graph
-        auto kern = three ? k_llt_stream<true, false, int> : k_llt_stream<false, false, int>;
-        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
-            CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, st, (const float*)bufs[k & 1], bufs[(k + 1) & 1], f,
-                                   lam_rof, lam_llt, tau, d, T.zchunk, (const StopCtl*)ctl.ctl(), ctl.partials()));
-            note_launch();
-            return OK;
-        }));
-        it = iters;
-    }
-    for (; it < iters; it++) {
-        const int check = ctl.is_check(it) ? 1 : 0;
+    auto launch = [&](const float* cur, float* nxt, int check, cudaStream_t st) -> cudaError_t {
+        if (T.pair)
+            return llt_pair_launch(T, cur, nxt, f, lam_rof, lam_llt, tau, d, ctl.ctl(), check, ctl.partials(), st);
         decltype(&k_llt_stream<true, true, int>) kern;
         if (d.n < (1LL << 31))
             kern = three ? (check ? k_llt_stream<true, true, int> : k_llt_stream<true, false, int>)
@@ -249,8 +234,22 @@ int llt_run(const float* f, float* u_out, float lam_rof, float lam_llt, int iter
         else
             kern = three ? (check ? k_llt_stream<true, true, long long> : k_llt_stream<true, false, long long>)
                          : (check ? k_llt_stream<false, true, long long> : k_llt_stream<false, false, long long>);
-        CILREG_CUDA(launch_pdl(kern, T.grid, T.block, 0, s, (const float*)bufs[it & 1], bufs[(it + 1) & 1], f,
-                               lam_rof, lam_llt, tau, d, T.zchunk, (const StopCtl*)ctl.ctl(), ctl.partials()));
+        return launch_pdl(kern, T.grid, T.block, 0, st, cur, nxt, f, lam_rof, lam_llt, tau, d, T.zchunk,
+                          (const StopCtl*)ctl.ctl(), ctl.partials());
+    };
+    int it = 0;
+    if (!ctl.checking() && d.n <= (1LL << 22)) {
+        // small volume, fixed count: launch overhead dominates, replay a graph
+        CILREG_TRY(run_replayed(iters, 64, s, [&](int k, cudaStream_t st, bool) -> int {
+            CILREG_CUDA(launch(bufs[k & 1], bufs[(k + 1) & 1], 0, st));
+            note_launch();
+            return OK;
+        }));
+        it = iters;
+    }
+    for (; it < iters; it++) {
+        const int check = ctl.is_check(it) ? 1 : 0;
+        CILREG_CUDA(launch(bufs[it & 1], bufs[(it + 1) & 1], check, s));
         note_launch();
         if (check) {
             CILREG_TRY(ctl.after_check(it, T.nblocks));

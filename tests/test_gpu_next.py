@@ -16,7 +16,10 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9), (130, 33, 35)]
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=str)
+LLT_SHAPES = SHAPES + [(67, 70, 10), (5, 31, 62), (3, 47, 2), (9, 1, 124), (4, 2, 90), (70, 29, 56)]
+
+
+@pytest.mark.parametrize("shape", LLT_SHAPES, ids=str)
 def test_llt_rof_matches_oracle_on_odd_shapes(shape):
     from ccpi.filters.regularisers import LLT_ROF
 
@@ -28,6 +31,28 @@ def test_llt_rof_matches_oracle_on_odd_shapes(shape):
         got = LLT_ROF(x, 0.02, 0.01, 80, 0.001, epsil, device="gpu", infovector=info)
         assert int(info[0]) == int(iref[0])
         assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-4)
+
+
+@pytest.mark.parametrize("shape", LLT_SHAPES, ids=str)
+def test_llt_rof_two_voxel_kernel_equals_one_voxel_kernel(shape, monkeypatch):
+    """3D volumes with an even row length run the two-voxel LLT-ROF kernel by
+    default; it computes the iteration of the one-voxel streaming kernel.  The
+    LLT term dxx / (|dxx| + 1e-12) is the sign of dxx wherever |dxx| >> 1e-12,
+    so a last-place rounding difference in a second difference near zero
+    moves a voxel by up to 2 tau lambdaLLT per iteration: the bar is the
+    oracle tests' 1e-4 of the range, not 1e-5."""
+    from ccpi.filters.regularisers import LLT_ROF
+
+    rng = np.random.default_rng(47 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil in (0.0, 1e-3):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = LLT_ROF(x, 0.02, 0.01, 80, 0.001, epsil, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_LLT_KERNEL", "stream")
+        b = LLT_ROF(x, 0.02, 0.01, 80, 0.001, epsil, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_LLT_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-4)
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=str)
