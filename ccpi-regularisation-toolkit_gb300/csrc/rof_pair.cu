@@ -212,6 +212,79 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
     if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
 }
 
+// 2D images: one plane per launch, the same pair arithmetic.  A CTA of
+// 16 x ROWS2 threads updates 30 x (ROWS2 - 2) pixels: U of the tile into
+// shared memory, the fluxes of every point into shared memory, the update of
+// the inner points (ROF_TV_core.c:102-160).  At 25-32 registers eight CTAs
+// fit on an SM, so a 512^2 image runs in one round of CTAs.
+constexpr int ROWS2 = 16;
+constexpr int TP2 = TW * ROWS2, NTP2 = PX * ROWS2;
+
+template <bool CHECK, bool LARR, bool ALIGNED>
+__global__ void __launch_bounds__(NTP2, 8)
+    k_rof_pair2d(const float* __restrict__ U, float* __restrict__ Un, const float* __restrict__ F,
+                 const float* __restrict__ lam_arr, float lam, float tau, Dims d, int, const StopCtl* ctl,
+                 double2* partials) {
+    __shared__ __align__(16) float sU[TP2];
+    __shared__ __align__(16) float sD1[TP2];
+    __shared__ __align__(16) float sD2[TP2];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int X = tile_x0(blockIdx.x) + 2 * tx;
+    const int y = blockIdx.y * (ROWS2 - 2) - 1 + ty;
+    const bool row_upd = ty >= 1 && ty <= ROWS2 - 2 && y >= 0 && y < ny;
+    const bool vx = row_upd && tx >= 1 && X >= 0 && X < nx;
+    const bool vy = row_upd && tx <= PX - 2 && X + 1 >= 0 && X + 1 < nx;
+    const int o = ty * TW + 2 * tx;
+    const int rowlo = ty * TW, rowhi = rowlo + TW - 1;
+    const int oxl = (X == 0) ? o + 1 : max(o - 1, rowlo);
+    const int oxh = (X + 2 == nx) ? o : min(o + 2, rowhi);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    yh = min(max(yh, 0), ROWS2 - 1);
+    yl = min(max(yl, 0), ROWS2 - 1);
+    const int oyh = yh * TW + 2 * tx, oyl = yl * TW + 2 * tx;
+    const int col = min(max(y, 0), ny - 1) * nx + min(max(X, 0), nx - 2);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+    // f and the lambda map never change during a run: loaded before waiting
+    // for the previous iteration (launch_pdl)
+    const float2 fv = ldg2(F + col);
+    const float2 lv = LARR ? ldg2(lam_arr + col) : splat(lam);
+    pdl_wait();
+    pdl_trigger();
+    if (ctl->stop) return;
+    const float2 u = ldg2(U + col);
+    st2(sU + o, u);
+    __syncthreads();
+    const float dxc = u.y - u.x;
+    const float2 xp = make_float2(dxc, sU[oxh] - u.y);
+    const float2 xm = make_float2(u.x - sU[oxl], dxc);
+    const float2 yp = sub2(ld2(sU + oyh), u), ym = sub2(u, ld2(sU + oyl));
+    const float2 mx2 = minmod_sq2(xp, xm), my2 = minmod_sq2(yp, ym);
+    const float2 EPS2 = splat(1.0e-8f);
+    const float2 d1 = normalise2(yp, add2(fma2(yp, yp, mx2), EPS2));
+    const float2 d2 = normalise2(xp, add2(fma2(xp, xp, my2), EPS2));
+    st2(sD1 + o, d1);
+    st2(sD2 + o, d2);
+    __syncthreads();
+    const float2 div = add2(sub2(d1, ld2(sD1 + oyl)), sub2(d2, make_float2(sD2[oxl], d2.x)));
+    const float2 t = sub2(u, fv);
+    const float2 un = fma2(splat(tau), fma2(lv, div, neg2(t)), u);
+    store_pair<ALIGNED>(Un + col, un, vx, vy);
+    float2 pa = splat(0.f), pb = splat(0.f);
+    if (CHECK) {
+        const float2 df = sub2(un, u);
+        const float2 dm = make_float2(vx ? df.x : 0.f, vy ? df.y : 0.f);
+        const float2 um = make_float2(vx ? un.x : 0.f, vy ? un.y : 0.f);
+        pa = mul2(dm, dm);
+        pb = mul2(um, um);
+        block_pair_partial<NTP2>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
+    }
+}
+
 // 16 rows: four CTAs per SM (32 warps in four independent barrier groups).
 // A 32-row tile has 7% fewer halo voxels but two CTAs per SM, and measured
 // 0.475 against 0.436 ms per 512^3 iteration.
@@ -224,6 +297,14 @@ PairKernel pick(bool check, bool larr, bool aligned) {
                      : (larr ? k_rof_pair<false, true, true, ROWS> : k_rof_pair<false, false, true, ROWS>);
     return check ? (larr ? k_rof_pair<true, true, false, ROWS> : k_rof_pair<true, false, false, ROWS>)
                  : (larr ? k_rof_pair<false, true, false, ROWS> : k_rof_pair<false, false, false, ROWS>);
+}
+
+PairKernel pick2d(bool check, bool larr, bool aligned) {
+    if (aligned)
+        return check ? (larr ? k_rof_pair2d<true, true, true> : k_rof_pair2d<true, false, true>)
+                     : (larr ? k_rof_pair2d<false, true, true> : k_rof_pair2d<false, false, true>);
+    return check ? (larr ? k_rof_pair2d<true, true, false> : k_rof_pair2d<true, false, false>)
+                 : (larr ? k_rof_pair2d<false, true, false> : k_rof_pair2d<false, false, false>);
 }
 
 // raise the dynamic shared-memory limit of every instantiation once
@@ -246,12 +327,19 @@ bool smem_ready() {
 bool rof_pair_applies(const Dims& d) {
     // CILREG_ROF_KERNEL=async (or reg, simple) keeps the one-voxel kernels
     const char* ek = getenv("CILREG_ROF_KERNEL");
-    return d.nz > 1 && d.nx % 2 == 0 && d.n < (1LL << 31) && !(ek && ek[0] != '\0' && ek[0] != 'p');
+    return d.nx % 2 == 0 && d.n < (1LL << 31) && !(ek && ek[0] != '\0' && ek[0] != 'p');
 }
 
 RofPlan rof_pair_plan(const Dims& d) {
     RofPlan T;
     T.pair = true;
+    if (d.nz == 1) {
+        T.block = dim3(PX, ROWS2, 1);
+        T.zchunk = 1;
+        T.grid = dim3(tiles_x(d.nx), (d.ny + ROWS2 - 3) / (ROWS2 - 2), 1);
+        T.nblocks = (long long)T.grid.x * T.grid.y;
+        return T;
+    }
     T.block = dim3(PX, ROWS, 1);
     const int gx = tiles_x(d.nx), gy = (d.ny + Geo<ROWS>::OYP - 1) / Geo<ROWS>::OYP;
     int resident = 0;
@@ -270,6 +358,11 @@ int rof_pair_step(const RofPlan& T, const float* cur, float* nxt, const float* f
     const bool larr = lam_arr != nullptr;
     const bool aligned =
         host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f) && (!larr || host_aligned8(lam_arr));
+    if (d.nz == 1) {
+        CILREG_CUDA(launch_pdl(pick2d(check != 0, larr, aligned), T.grid, T.block, 0, s, cur, nxt, f, lam_arr, lam,
+                               tau, d, 1, ctl, partials));
+        return OK;
+    }
     if (!smem_ready())
         return fail(ERR_CUDA, __FILE__, __LINE__, "cannot raise the shared-memory limit of k_rof_pair");
     CILREG_CUDA(launch_pdl(pick(check != 0, larr, aligned), T.grid, T.block, Geo<ROWS>::SMEM, s, cur, nxt, f,

@@ -14,8 +14,9 @@ struct RofPlan {
 
 RofPlan rof_tiled_plan(const Dims& d);
 
-// 3D volumes with nx even and fewer than 2^31 voxels run k_rof_pair
-// (CILREG_ROF_KERNEL=async, reg or simple select a one-voxel kernel)
+// volumes and images with nx even and fewer than 2^31 voxels run k_rof_pair
+// (3D) or k_rof_pair2d (CILREG_ROF_KERNEL=async, reg or simple select a
+// one-voxel kernel)
 bool rof_pair_applies(const Dims& d);
 RofPlan rof_pair_plan(const Dims& d);
 int rof_pair_step(const RofPlan& T, const float* cur, float* nxt, const float* f, const float* lam_arr, float lam,

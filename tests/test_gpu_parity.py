@@ -376,11 +376,13 @@ def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
                                    (130, 33, 35), (151, 12, 31), (67, 70, 10), (130, 33, 64), (5, 31, 62),
-                                   (3, 47, 2), (9, 61, 124), (4, 2, 90)], ids=str)
+                                   (3, 47, 2), (9, 61, 124), (4, 2, 90), (2, 64), (45, 2), (130, 96), (1, 70)],
+                         ids=str)
 def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
     """The 2.5D streaming ROF kernels and the per-voxel kernel compute the same
-    iteration (3D volumes with an even row length run the two-voxel kernel by
-    default; odd rows and the tile edges at 30 n - 1 and 30 n + 28 included)."""
+    iteration (volumes and images with an even row length run the two-voxel
+    kernels by default; odd rows and the tile edges at 30 n - 1 and 30 n + 28
+    included)."""
     from ccpi.filters.regularisers import ROF_TV
 
     rng = np.random.default_rng(11 + sum(shape))
@@ -544,12 +546,15 @@ def test_rof_2d_overlapped_halo_blocks_equal_single_iterations(shape, depth, mon
     """2D ROF-TV at fixed counts runs `depth` iterations per launch on tiles
     with overlapped halos; the result equals one launch per iteration, for
     iteration counts that are not multiples of the depth, with a scalar and
-    a per-pixel lambda."""
+    a per-pixel lambda.  The single iterations are those of the one-voxel
+    kernel (k_rof_stream), whose arithmetic the overlapped-halo kernel
+    repeats."""
     from ccpi.filters.regularisers import ROF_TV
 
     rng = np.random.default_rng(41 + sum(shape))
     x = rng.random(shape).astype(np.float32)
     lam_map = (0.01 + 0.03 * rng.random(shape)).astype(np.float32)
+    monkeypatch.setenv("CILREG_ROF_KERNEL", "async")
     monkeypatch.setenv("CILREG_ROF_TB", depth)
     for iters in (37, 120):
         a = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
