@@ -54,6 +54,18 @@ __device__ __forceinline__ float ldg(const float* p, long long v) { return __ldg
 
 __device__ __forceinline__ float sgnf(float x) { return (float)((x > 0.0f) - (x < 0.0f)); }
 
+// flags between CTAs of one launch: an acquire load and a release store at
+// GPU scope
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // block-level FP64 pair reduction -> one double2 partial per CTA
 // ---------------------------------------------------------------------------

@@ -269,16 +269,6 @@ __global__ void __launch_bounds__(NT, 3) k_fgp_stream_batch(const FgpBatchVol* _
 // the finalize kernel) and releases the iteration.  State written within the
 // launch is read through L2 (ld.global.cg), never from a stale L1 line.
 
-__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release_gpu(int* p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // one volume's stopping check by the whole CTA (NT = 512 threads): the sums of
 // k_finalize_batch's 1024-thread order (thread t and t + 512 of that kernel
 // are this thread's two chains), so the relative change is bit-identical

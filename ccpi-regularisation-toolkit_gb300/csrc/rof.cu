@@ -157,6 +157,21 @@ int rof_run(const float* f, float* u_out, const float* lam_arr, float lam, int i
     float* bufs[2] = {u_out, alt};
     CILREG_CUDA(cudaMemcpyAsync(u_out, u_init ? u_init : f, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
     int it = 0;
+    if (!ctl.checking() && !use_simple_kernel() && rof_tb2d_depth(d, iters) == 0 &&
+        rof_persist2d_applies(d, iters)) {
+        // 2D image, fixed count: every iteration in one persistent launch
+        const long long tiles = rof_persist2d_tiles(d);
+        int* flags = (int*)scratch.bytes(sizeof(int) * (size_t)(tiles + 1));
+        if (!flags) return scratch.status();
+        CILREG_TRY(rof_persist2d_run(u_out, alt, f, lam_arr, lam, tau, iters, d, flags, flags + tiles, s));
+        note_launch();
+        int err = 0;
+        CILREG_CUDA(cudaMemcpyAsync(&err, flags + tiles, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CILREG_CUDA(cudaStreamSynchronize(s));
+        if (err) return fail(ERR_CUDA, __FILE__, __LINE__, "a wait between the tiles of k_rof_persist2d ran out");
+        if (iters & 1) CILREG_CUDA(cudaMemcpyAsync(u_out, alt, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s));
+        return ctl.finish(info);
+    }
     const int depth = ctl.checking() ? 0 : rof_tb2d_depth(d, iters);
     if (depth > 0 && !use_simple_kernel()) {
         // 2D image, fixed count: `depth` iterations per launch on tiles with

@@ -35,4 +35,14 @@ int rof_tb2d_depth(const Dims& d, int iters);
 int rof_tb2d_step(const float* cur, float* nxt, const float* f, const float* lam_arr, float lam, float tau,
                   const Dims& d, int depth, cudaStream_t s);
 
+// 2D images at a fixed count: all iterations in one cooperative launch of
+// k_rof_persist2d (rof_persist.cu) when every 32 x 64 tile can be resident at
+// once; opt-in, CILREG_ROF_PERSIST=1 (slower than graph-replayed launches)
+bool rof_persist2d_applies(const Dims& d, int iters);
+long long rof_persist2d_tiles(const Dims& d);
+// U^0 in g0; U^iters ends in g[iters & 1]; flags: one int per tile, error one
+// int (set when a wait between tiles ran out)
+int rof_persist2d_run(float* g0, float* g1, const float* f, const float* lam_arr, float lam, float tau, int iters,
+                      const Dims& d, int* flags, int* error, cudaStream_t s);
+
 }  // namespace cilreg

@@ -612,3 +612,30 @@ def test_rof_pair_kernel_with_arrays_off_8_byte_alignment(lam_map):
     # the oracle at the iteration count the stopping rule gave
     ref, _ = O.rof_tv(x, lm if lam_map else 0.02, int(ia[0]), 0.001, 0.0)
     assert np.max(np.abs(a - ref)) <= rel_tol(ref, 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(512, 512), (37, 95), (1, 70), (70, 1), (2, 2), (130, 97), (64, 32), (65, 33),
+                                   (300, 200), (129, 256)], ids=str)
+def test_rof_2d_persistent_launch_equals_one_launch_per_iteration(shape, monkeypatch):
+    """2D ROF-TV at fixed counts can run every iteration in one persistent
+    launch (CILREG_ROF_PERSIST=1; tiles exchange their borders through global
+    memory and per-tile flags); the result equals one launch of the one-voxel
+    kernel per iteration, bit for bit, with a scalar and a per-pixel lambda,
+    for odd and even counts."""
+    from ccpi.filters.regularisers import ROF_TV
+
+    rng = np.random.default_rng(53 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    lam_map = (0.01 + 0.03 * rng.random(shape)).astype(np.float32)
+    for iters in (2, 37, 120):
+        monkeypatch.setenv("CILREG_ROF_PERSIST", "1")
+        a = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
+        am = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")  # lambda map: the C-OMP ABI, run on the GPU
+        monkeypatch.setenv("CILREG_ROF_PERSIST", "0")
+        monkeypatch.setenv("CILREG_ROF_KERNEL", "async")
+        b = ROF_TV(x, 0.02, iters, 0.001, 0.0, device="gpu")
+        bm = ROF_TV(x, lam_map, iters, 0.001, 0.0, device="cpu")
+        monkeypatch.delenv("CILREG_ROF_PERSIST")
+        monkeypatch.delenv("CILREG_ROF_KERNEL")
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(am, bm)
