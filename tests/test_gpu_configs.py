@@ -8,6 +8,8 @@ the library in FP64, so such a check can fall on either side).
 Cases (sizes and parameters of the plain, batched and served workloads):
   * FGP-TV 3D 512^3 (lambda 0.03, iso, nonneg, epsil 1e-6) for 60 iterations:
     the benchmark's tensor-copy kernel with twelve stopping-check launches;
+  * ROF-TV, NDF, Diff4th and LLT-ROF 3D 512^3 for 10 iterations through the
+    two-voxel kernels;
   * FGP-TV and PD-TV 3D 256^3, up to 500 iterations, epsil 1e-6 (PD with
     Lipschitz constant 8), FGP also through the tensor-copy kernel;
   * SB-TV, TGV, NDF, Diff4th, ROF-TV, LLT-ROF 3D 256^3 for fixed counts with
@@ -73,6 +75,30 @@ def test_fgp_512_benchmark_kernel_with_stopping_checks(vol512, monkeypatch):
     # the reference's sequential FP32 sum of 2^27 squares is biased low; it
     # stays within 25% of the exact value at this size
     assert abs(float(ref_info[1]) - re) <= 0.25 * re
+
+
+CASES_512 = {
+    "ROF": (lambda x: O.rof_tv(x, 0.02, 10, 0.001, 0.0),
+            lambda R, x: R.ROF_TV(x, 0.02, 10, 0.001, 0.0, device="gpu")),
+    "NDF_Huber": (lambda x: O.ndf(x, 0.02, 0.02, 10, 0.01, 1, 0.0, jacobi=True),
+                  lambda R, x: R.NDF(x, 0.02, 0.02, 10, 0.01, 1, 0.0, device="gpu")),
+    "Diff4th": (lambda x: O.diff4th(x, 0.8, 0.02, 10, 1e-4, 0.0),
+                lambda R, x: R.Diff4th(x, 0.8, 0.02, 10, 1e-4, 0.0, device="gpu")),
+    "LLT_ROF": (lambda x: O.llt_rof(x, 0.02, 0.01, 10, 0.001, 0.0),
+                lambda R, x: R.LLT_ROF(x, 0.02, 0.01, 10, 0.001, 0.0, device="gpu")),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES_512))
+def test_two_voxel_kernels_512_against_oracle(vol512, name):
+    """The two-voxel kernels at the size the per-regulariser figures are
+    quoted on (512^3, the default kernels; 10 iterations)."""
+    from ccpi.filters import regularisers as R
+
+    oracle_fn, gpu_fn = CASES_512[name]
+    ref, _ = oracle_fn(vol512)
+    out = gpu_fn(R, vol512)
+    _assert_close(out, ref, f"{name} 512^3")
 
 
 # --------------------------------------------------------------------------- 256^3
