@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
 // 16 x ROWS2 threads updates 30 x (ROWS2 - 2) pixels: U of the tile into
 // shared memory, the fluxes of every point into shared memory, the update of
 // the inner points (ROF_TV_core.c:102-160).  At 25-32 registers eight CTAs
-// fit on an SM, so a 512^2 image runs in one round of CTAs.
+// fit on an SM, so a 512^2 image runs in one wave of CTAs.
 constexpr int ROWS2 = 16;
 constexpr int TP2 = TW * ROWS2, NTP2 = PX * ROWS2;
 

@@ -3,7 +3,7 @@
 //
 // A 512^2 image takes about 2.4 us per iteration as one launch per iteration
 // replayed from a CUDA graph, mostly the latency of a launch and of its
-// single round of CTAs, not its work.  Here each CTA keeps one 32 x 64 tile
+// single wave of CTAs, not its work.  Here each CTA keeps one 32 x 64 tile
 // of U in shared memory for the whole run and exchanges only the tile's
 // border with its eight neighbours through global memory (L2):
 //   1. wait until the neighbour tiles have published iteration t (a flag per
