@@ -202,6 +202,67 @@ __global__ void __launch_bounds__(NTP, 4)
     if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
 }
 
+// 2D images: one plane per launch, the same pair arithmetic (the 2D path of
+// k_ndf_stream: Diffusion_core.c:140-239).  A CTA of 16 x 16 threads updates
+// 30 x 14 pixels; at under 40 registers six CTAs fit on an SM, so a 512^2
+// image runs in one wave of CTAs.
+template <int PEN, bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP, 6)
+    k_ndf_pair2d(const float* __restrict__ U, float* __restrict__ Un, const float* __restrict__ F, float lam,
+                 float sg, float isg, float tau, Dims d, int, const StopCtl* ctl, double2* partials) {
+    __shared__ __align__(16) float sU[TP];
+    __shared__ __align__(16) float sFx[TP];
+    __shared__ __align__(16) float sFy[TP];
+    const float2 isg2 = splat(isg), lam2 = splat(lam), tau2 = splat(tau);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int X = tile_x0(blockIdx.x) + 2 * tx;
+    const int y = blockIdx.y * OYP - 1 + ty;
+    const bool row_upd = ty >= 1 && ty <= TH - 2 && y >= 0 && y < ny;
+    const bool vx = row_upd && tx >= 1 && X >= 0 && X < nx;
+    const bool vy = row_upd && tx <= PX - 2 && X + 1 >= 0 && X + 1 < nx;
+    const int o = ty * TW + 2 * tx;
+    const int rowlo = ty * TW, rowhi = rowlo + TW - 1;
+    const int oxh = (X + 2 == nx) ? o : min(o + 2, rowhi);
+    const int oxw = (X == 0) ? o : max(o - 1, rowlo);
+    const float2 wsg2 = make_float2((X == 0) ? 1.0f : -1.0f, -1.0f);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    yh = min(max(yh, 0), TH - 1);
+    const int oyh = yh * TW + 2 * tx;
+    const int oys = (y == 0) ? o : max(ty - 1, 0) * TW + 2 * tx;
+    const float2 ssg2 = splat((y == 0) ? 1.0f : -1.0f);
+    const int col = min(max(y, 0), ny - 1) * nx + min(max(X, 0), nx - 2);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+    const float2 fv = ldg2(F + col);  // f never changes during a run: loaded before the wait
+    pdl_wait();
+    pdl_trigger();
+    if (ctl->stop) return;
+    const float2 u = ldg2(U + col);
+    st2(sU + o, u);
+    __syncthreads();
+    const float2 fx = flux2<PEN>(make_float2(u.y - u.x, sU[oxh] - u.y), sg, isg2);
+    const float2 fy = flux2<PEN>(sub2(ld2(sU + oyh), u), sg, isg2);
+    st2(sFx + o, fx);
+    st2(sFy + o, fy);
+    __syncthreads();
+    // e + w + n + s (Diffusion_core.c:160-164)
+    float2 sum = fma2(wsg2, make_float2(sFx[oxw], fx.x), fx);
+    sum = add2(sum, fy);
+    sum = fma2(ssg2, ld2(sFy + oys), sum);
+    const float2 t = sub2(u, fv);
+    const float2 un = fma2(tau2, fma2(lam2, sum, neg2(t)), u);
+    store_pair<ALIGNED>(Un + col, un, vx, vy);
+    if (CHECK) {
+        const float2 df = sub2(un, u);
+        const float2 dm = make_float2(vx ? df.x : 0.f, vy ? df.y : 0.f);
+        const float2 um = make_float2(vx ? un.x : 0.f, vy ? un.y : 0.f);
+        block_pair_partial<NTP>(dm.x * dm.x + dm.y * dm.y, um.x * um.x + um.y * um.y, partials, block_slot());
+    }
+}
+
 using PairKernel = decltype(&k_ndf_pair<0, false, true>);
 
 template <int PEN>
@@ -218,6 +279,24 @@ PairKernel pick(int pen, bool check, bool aligned) {
         case 3: return pick_pen<3>(check, aligned);
         case 4: return pick_pen<4>(check, aligned);
         case 5: return pick_pen<5>(check, aligned);
+        default: return nullptr;
+    }
+}
+
+template <int PEN>
+PairKernel pick2d_pen(bool check, bool aligned) {
+    if (aligned) return check ? k_ndf_pair2d<PEN, true, true> : k_ndf_pair2d<PEN, false, true>;
+    return check ? k_ndf_pair2d<PEN, true, false> : k_ndf_pair2d<PEN, false, false>;
+}
+
+PairKernel pick2d(int pen, bool check, bool aligned) {
+    switch (pen) {
+        case 0: return pick2d_pen<0>(check, aligned);
+        case 1: return pick2d_pen<1>(check, aligned);
+        case 2: return pick2d_pen<2>(check, aligned);
+        case 3: return pick2d_pen<3>(check, aligned);
+        case 4: return pick2d_pen<4>(check, aligned);
+        case 5: return pick2d_pen<5>(check, aligned);
         default: return nullptr;
     }
 }
@@ -242,13 +321,20 @@ bool smem_ready() {
 bool ndf_pair_applies(const Dims& d) {
     // CILREG_NDF_KERNEL=stream (or simple) keeps a one-voxel kernel
     const char* e = getenv("CILREG_NDF_KERNEL");
-    return d.nz > 1 && d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
+    return d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
 }
 
 NdfPlan ndf_pair_plan(const Dims& d) {
     NdfPlan T;
     T.use = true;
     T.pair = true;
+    if (d.nz == 1) {
+        T.block = dim3(PX, ROWS, 1);
+        T.zchunk = 1;
+        T.grid = dim3(tiles_x(d.nx), (d.ny + OYP - 1) / OYP, 1);
+        T.nblocks = (long long)T.grid.x * T.grid.y;
+        return T;
+    }
     T.block = dim3(PX, ROWS, 1);
     const int gx = tiles_x(d.nx), gy = (d.ny + OYP - 1) / OYP;
     int resident = 0;
@@ -267,6 +353,12 @@ int ndf_pair_step(const NdfPlan& T, int pen, const float* cur, float* nxt, const
                   float isg, float tau, const Dims& d, const StopCtl* ctl, int check, double2* partials,
                   cudaStream_t s) {
     if (pen < 0 || pen > 5) return fail(ERR_ARG, __FILE__, __LINE__, "penalty %d out of range", pen);
+    if (d.nz == 1) {
+        const bool al = host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f);
+        CILREG_CUDA(launch_pdl(pick2d(pen, check != 0, al), T.grid, T.block, 0, s, cur, nxt, f, lam, sg, isg, tau, d,
+                               1, ctl, partials));
+        return OK;
+    }
     if (!smem_ready())
         return fail(ERR_CUDA, __FILE__, __LINE__, "cannot raise the shared-memory limit of k_ndf_pair");
     const bool aligned = host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f);

@@ -44,9 +44,10 @@ struct NdfPlan {
     bool pair = false;  // the two-voxels-per-thread kernel (ndf_pair.cu)
 };
 
-// the plan of the kernel that runs for `d`: 3D volumes with nx even and
-// fewer than 2^31 voxels run k_ndf_pair, other volumes below 2^31 voxels
-// k_ndf_stream (CILREG_NDF_KERNEL=stream or simple select a one-voxel kernel)
+// the plan of the kernel that runs for `d`: volumes and images with nx even
+// and fewer than 2^31 voxels run k_ndf_pair (3D) or k_ndf_pair2d, others
+// below 2^31 voxels k_ndf_stream (CILREG_NDF_KERNEL=stream or simple select a
+// one-voxel kernel)
 NdfPlan ndf_stream_plan(const Dims& d);
 bool ndf_pair_applies(const Dims& d);
 NdfPlan ndf_pair_plan(const Dims& d);

@@ -406,13 +406,14 @@ def test_rof_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
-                                   (130, 33, 35), (67, 70, 10), (5, 31, 62), (3, 47, 2), (9, 1, 124), (4, 2, 90)],
+                                   (130, 33, 35), (67, 70, 10), (5, 31, 62), (3, 47, 2), (9, 1, 124), (4, 2, 90),
+                                   (2, 64), (45, 2), (130, 96), (1, 70)],
                          ids=str)
 @pytest.mark.parametrize("penalty", [0, 1, 2, 3, 4, 5])
 def test_ndf_streaming_kernel_equals_per_voxel_kernel(shape, penalty, monkeypatch):
     """The 2.5D streaming NDF kernels (one flux per face, used with both signs;
-    3D volumes with an even row length run the two-voxel kernel by default)
-    and the per-voxel kernel (six fluxes per voxel) compute the same
+    volumes and images with an even row length run the two-voxel kernels by
+    default) and the per-voxel kernel (six fluxes per voxel) compute the same
     iteration."""
     from ccpi.filters.regularisers import NDF
 
