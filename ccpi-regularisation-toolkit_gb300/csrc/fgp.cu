@@ -125,7 +125,13 @@ int fgp_run(const float* f, float* u_out, float lam, int iters, float epsil, int
     const int R = TP.use ? 4 : 3;
     // the tensor-copy kernel: same tiles, z chunks balanced for its own occupancy
     bool tma = T.use && !TP.use && fgp_tma_usable(d);
-    if (tma) T = fgp_tiled_plan(d, fgp_tma_resident());
+    if (tma) {
+        T = fgp_tiled_plan(d, fgp_tma_resident());
+    } else if (T.use && !TP.use) {
+        // below the tensor-copy kernel's sizes: two voxels per thread
+        const TiledPlan X = fgp_x2_plan(d);
+        if (X.use) T = X;
+    }
     IterControl ctl(s, scratch, iters, epsil, T.use ? T.nblocks : num_blocks(L));
     CILREG_TRY(ctl.status());
     float* ring[4][3] = {};

@@ -21,6 +21,7 @@
 #include "fgp_tiled.cuh"
 
 #include <stdlib.h>
+#include <string.h>
 
 namespace cilreg {
 
@@ -466,7 +467,7 @@ int fgp_advance_base(int* base, int by, cudaStream_t s) {
 TiledPlan fgp_tiled_plan(const Dims& d, int resident_ctas_per_sm) {
     TiledPlan T;
     const char* e = getenv("CILREG_FGP_KERNEL");
-    T.use = !(e && e[0] == 's');  // "simple" selects the per-voxel kernel of fgp.cu
+    T.use = !(e && strcmp(e, "simple") == 0);  // "simple" selects the per-voxel kernel of fgp.cu
     T.block = dim3(BX, BY, 1);
     if (d.nz > 1) {
         // one volume: balance the CTAs over the SMs (the batched path packs
@@ -486,6 +487,9 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
                    const float* const* b, const float* carr, const int* cbase, int coff) {
+    if (T.x2 && !b)
+        return fgp_x2_step(T, pc, po, pn, f, u, lam, c, multip, nonneg, aniso, write_u, write_p, check, d, ctl,
+                           partials, s, carr, cbase, coff);
     TiledArgs a;
     a.carr = carr;
     a.cbase = cbase;

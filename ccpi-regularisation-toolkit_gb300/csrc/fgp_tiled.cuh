@@ -10,6 +10,7 @@ struct TiledPlan {
     dim3 grid, block;
     long long nblocks = 0;
     int zchunk = 0;
+    bool x2 = false;  // the two-voxels-per-thread kernel (fgp_x2.cu)
 };
 
 // z chunks balanced for `resident_ctas_per_sm` CTAs per SM (0: those of k_fgp_stream)
@@ -27,6 +28,16 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
                    int coff = 0);
 // *base += by on the device (one thread)
 int fgp_advance_base(int* base, int by, cudaStream_t s);
+
+// The iteration with two voxels per thread (fgp_x2.cu): 3D volumes with nx
+// even and fewer than 2^31 voxels (CILREG_FGP_KERNEL=stream or simple keep a
+// one-voxel kernel; use is false otherwise).  fgp_tiled_step runs it for a
+// plan with x2 set (not for FGP-dTV).
+TiledPlan fgp_x2_plan(const Dims& d);
+int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
+                const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
+                int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
+                const float* carr, const int* cbase, int coff);
 
 // Two iterations k, k+1 in one streaming pass (fgp_pair.cu; 3D only).
 struct PairPlan {

@@ -1,0 +1,241 @@
+// FGP-TV 3D iteration with two voxels per thread along x (arithmetic
+// FGP_TV_core.c:220-269, projection utils.c:180-213).
+//
+// The scheme of k_fgp_stream (R and U formed once per voxel, P of plane k-1
+// from U's forward differences one plane behind, two barriers per plane, the
+// next plane's inputs loaded one plane ahead into registers) with the work
+// of a thread doubled along x, as k_rof_pair does for ROF-TV: each thread
+// holds the voxel pair (x, x+1), x even, so that the seven inputs, R, U and
+// the outputs move in 8-byte accesses, offsets and loop control serve two
+// voxels, and the additions, multiplications and fused multiply-adds of both
+// voxels issue as paired FP32 instructions.  The projection's reciprocal
+// square roots and divisions stay per voxel.
+//
+// It runs on volumes of 2^21 to 2^25 voxels, where k_fgp_stream is bound by
+// instruction issue and by the latency of its waves rather than by DRAM (the
+// larger ones stage their inputs by tensor copies, fgp_tma.cu): 128^3 18.1
+// against 20.8 us per iteration, 256^3 115.7 against 122.6, 320^3 218.6
+// against 229.9.
+//
+// A CTA of 16 x 16 threads holds a 32 x 16 tile with the one-voxel halo of
+// k_fgp_stream: U on points 1..31, P written on the inner 30 x 14 (whole
+// pairs but for the first voxel of thread 0 and the second of thread 15).
+// Tile x origins are even (x0 = 30 bx - 2).  Needs nx even; arrays off
+// 8-byte alignment run the 4-byte instantiation.
+#include <stdlib.h>
+
+#include "fgp_tiled.cuh"
+#include "pair.cuh"
+
+namespace cilreg {
+
+namespace {
+
+using namespace pair;
+
+constexpr int ROWS = 16;
+constexpr int NTP = PX * ROWS, OYP = ROWS - 2;
+constexpr int ZCHUNK = 64;
+
+struct X2Args {
+    const float* pc[3];
+    const float* po[3];
+    float* pn[3];
+    const float* f;
+    float* u;
+    float lam, c, multip;
+    int nonneg, aniso, write_u, write_p;
+    const float* carr;  // momentum from device memory (graph replays): carr[*cbase + coff]
+    const int* cbase;
+    int coff;
+};
+
+template <bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, const StopCtl* ctl,
+                                                   double2* partials) {
+    __shared__ __align__(16) float sR1[ROWS * TW];
+    __shared__ __align__(16) float sR2[ROWS * TW];
+    __shared__ __align__(16) float sU[2][ROWS * TW];
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny, nz = d.nz;
+    const int X = tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first voxel
+    const int y = blockIdx.y * OYP - 1 + ty;
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, nz);
+    // both voxels lie in the volume or neither does (nx even, X even)
+    const bool in_xy = X >= 0 && X < nx && y >= 0 && y < ny;
+    const bool urow = in_xy && ty >= 1;
+    const bool ux = urow && tx >= 1;  // U of the first voxel is needed (point 2 tx >= 1)
+    const bool prow = urow && ty <= OYP;
+    const bool vx = prow && tx >= 1;       // P of the first voxel written
+    const bool vy = prow && tx <= PX - 2;  // P of the second voxel written
+    const bool xlast = (X + 2 == nx), ylast = (y == ny - 1);
+    const int o = ty * TW + 2 * tx;
+    const int oxl = max(o - 1, ty * TW);                 // R1 at x-1 of the first voxel (0 outside: loads)
+    const int oxh = min(o + 2, ty * TW + TW - 1);        // U at x+1 of the second voxel
+    const int oyl = max(ty - 1, 0) * TW + 2 * tx;        // R2 at y-1
+    const int oyh = min(ty + 1, ROWS - 1) * TW + 2 * tx;  // U at y+1
+    const int col = in_xy ? (y * nx + X) : 0;
+    const int sxy = d.sxy;
+    const float2 lam2 = splat(a.lam), mp2 = splat(a.multip);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+
+    // prefetch registers for one plane
+    float2 c1 = splat(0.f), o1 = splat(0.f), c2 = splat(0.f), o2 = splat(0.f), c3 = splat(0.f), o3 = splat(0.f);
+    float2 fv = splat(0.f);
+    auto load_plane = [&](int k) {
+        if (in_xy && k >= 0 && k < nz) {
+            const int v = k * sxy + col;
+            c1 = ldg2(a.pc[0] + v);
+            o1 = ldg2(a.po[0] + v);
+            c2 = ldg2(a.pc[1] + v);
+            o2 = ldg2(a.po[1] + v);
+            c3 = ldg2(a.pc[2] + v);
+            o3 = ldg2(a.po[2] + v);
+            fv = ldg2(a.f + v);
+        } else {
+            c1 = o1 = c2 = o2 = c3 = o3 = fv = splat(0.f);
+        }
+    };
+    float2 r1p = splat(0.f), r2p = splat(0.f), r3p = splat(0.f), up = splat(0.f);
+    float2 uo = splat(0.f);
+    float2 pa = splat(0.f), pb = splat(0.f);
+    const float2 cm = splat(a.carr ? a.carr[*a.cbase + a.coff] : a.c);
+    load_plane(z0 - 1);
+    for (int k = z0 - 1; k <= z1; ++k) {
+        // 1. R of plane k (FGP_TV_core.c:257-269); start loading plane k+1
+        const float2 r1 = fma2(cm, sub2(c1, o1), c1);
+        const float2 r2 = fma2(cm, sub2(c2, o2), c2);
+        const float2 r3 = fma2(cm, sub2(c3, o3), c3);
+        const float2 fk = fv;
+        if (k < z1) load_plane(k + 1);
+        float2 uo_next = splat(0.f);
+        if (CHECK && prow && k >= z0 && k < z1) {
+            const float* q = a.u + (k * sxy + col);
+            uo_next = ALIGNED ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
+        }
+        st2(sR1 + o, r1);
+        st2(sR2 + o, r2);
+        __syncthreads();
+        // 2. U of plane k = f - lambda div_b R (FGP_TV_core.c:220-236, clamp :129)
+        float2 u = splat(0.f);
+        if (urow && k >= z0 && k < nz) {
+            const float2 r1l = make_float2(sR1[oxl], r1.x);
+            const float2 s = sub2(sub2(sub2(add2(add2(r1, r2), r3), r1l), ld2(sR2 + oyl)), r3p);
+            u = fma2(neg2(lam2), s, fk);
+            if (a.nonneg) u = make_float2(u.x < 0.f ? 0.f : u.x, u.y < 0.f ? 0.f : u.y);
+            if (!ux) u.x = 0.f;
+        }
+        st2(sU[k & 1] + o, u);
+        __syncthreads();
+        // 3. P^k of plane k-1 (FGP_TV_core.c:237-256, utils.c:180-213)
+        const int kp = k - 1;
+        if ((vx || vy) && kp >= z0) {
+            const int v = kp * sxy + col;
+            if (CHECK) {
+                const float2 df = sub2(up, uo);
+                const float2 dm = make_float2(vx ? df.x : 0.f, vy ? df.y : 0.f);
+                const float2 um = make_float2(vx ? up.x : 0.f, vy ? up.y : 0.f);
+                pa = fma2(dm, dm, pa);
+                pb = fma2(um, um, pb);
+            }
+            if (a.write_u) store_pair<ALIGNED>(a.u + v, up, vx, vy);
+            if (a.write_p) {
+                const float* Up = sU[kp & 1];
+                float2 g1 = make_float2(up.x - up.y, xlast ? 0.f : up.y - Up[oxh]);
+                const float2 g2 = ylast ? splat(0.f) : sub2(up, ld2(Up + oyh));
+                const float2 g3 = (kp != nz - 1) ? sub2(up, u) : splat(0.f);
+                float2 p1 = fma2(mp2, g1, r1p);
+                float2 p2 = fma2(mp2, g2, r2p);
+                float2 p3 = fma2(mp2, g3, r3p);
+                if (!a.aniso) {
+                    const float2 den = fma2(p3, p3, fma2(p2, p2, mul2(p1, p1)));
+                    const float2 sq = make_float2((den.x > 1.f) ? rsqrtf(den.x) : 1.f,
+                                                  (den.y > 1.f) ? rsqrtf(den.y) : 1.f);
+                    p1 = mul2(p1, sq);
+                    p2 = mul2(p2, sq);
+                    p3 = mul2(p3, sq);
+                } else {
+                    auto an = [](float p) { return p / fmaxf(fabsf(p), 1.f); };
+                    p1 = make_float2(an(p1.x), an(p1.y));
+                    p2 = make_float2(an(p2.x), an(p2.y));
+                    p3 = make_float2(an(p3.x), an(p3.y));
+                }
+                store_pair<ALIGNED>(a.pn[0] + v, p1, vx, vy);
+                store_pair<ALIGNED>(a.pn[1] + v, p2, vx, vy);
+                store_pair<ALIGNED>(a.pn[2] + v, p3, vx, vy);
+            }
+        }
+        r1p = r1;
+        r2p = r2;
+        r3p = r3;
+        up = u;
+        uo = uo_next;
+    }
+    if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
+}
+
+using X2Kernel = decltype(&k_fgp_x2<false, true>);
+
+X2Kernel pick(bool check, bool aligned) {
+    if (aligned) return check ? k_fgp_x2<true, true> : k_fgp_x2<false, true>;
+    return check ? k_fgp_x2<true, false> : k_fgp_x2<false, false>;
+}
+
+}  // namespace
+
+TiledPlan fgp_x2_plan(const Dims& d) {
+    TiledPlan T;
+    // CILREG_FGP_KERNEL=stream (or simple) keeps a one-voxel kernel
+    const char* e = getenv("CILREG_FGP_KERNEL");
+    // from 2^21 voxels (128^3): below it the one-voxel kernel's wave is as
+    // fast (96^3: 11.8 against 13.0 us per iteration)
+    if (!(d.nz > 1 && d.nx % 2 == 0 && d.n >= (1LL << 21) && d.n < (1LL << 31) &&
+          !(e && e[0] != '\0' && e[0] != 'x')))
+        return T;
+    T.use = true;
+    T.x2 = true;
+    T.block = dim3(PX, ROWS, 1);
+    static const int resident = resident_ctas(k_fgp_x2<false, true>, NTP);
+    const int gx = tiles_x(d.nx), gy = (d.ny + OYP - 1) / OYP;
+    T.zchunk = wave_zchunk((long long)gx * gy, d.nz, resident, 2, ZCHUNK);
+    T.grid = dim3(gx, gy, (d.nz + T.zchunk - 1) / T.zchunk);
+    T.nblocks = (long long)T.grid.x * T.grid.y * T.grid.z;
+    return T;
+}
+
+int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
+                const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
+                int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
+                const float* carr, const int* cbase, int coff) {
+    X2Args a;
+    bool aligned = host_aligned8(f) && host_aligned8(u);
+    for (int i = 0; i < 3; i++) {
+        a.pc[i] = pc[i];
+        a.po[i] = po[i];
+        a.pn[i] = pn[i];
+        aligned = aligned && host_aligned8(pc[i]) && host_aligned8(po[i]) && host_aligned8(pn[i]);
+    }
+    a.f = f;
+    a.u = u;
+    a.lam = lam;
+    a.c = c;
+    a.multip = multip;
+    a.nonneg = nonneg;
+    a.aniso = aniso;
+    a.write_u = write_u;
+    a.write_p = write_p;
+    a.carr = carr;
+    a.cbase = cbase;
+    a.coff = coff;
+    CILREG_CUDA(launch_pdl(pick(check != 0, aligned), T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
+    return OK;
+}
+
+}  // namespace cilreg

@@ -216,21 +216,31 @@ def test_fgp_512_full_size_against_port():
     assert np.max(np.abs(out - ref)) <= rel_tol(ref, TOL)
 
 
-@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (10, 16, 22), (67, 70, 9), (130, 33, 35)], ids=str)
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (10, 16, 22), (67, 70, 9), (130, 33, 35), (67, 70, 10),
+                                   (5, 31, 62), (33, 250, 258), (40, 231, 230), (17, 4097, 32)], ids=str)
 def test_fgp_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
-    """The 2.5D streaming FGP kernel and the per-voxel kernel compute the same iteration."""
+    """The 2.5D streaming FGP kernels and the per-voxel kernel compute the same
+    iteration (3D volumes of 2^21 to 2^25 voxels with an even row length run
+    the two-voxel kernel by default, CILREG_FGP_KERNEL=stream the one-voxel
+    one)."""
     from ccpi.filters.regularisers import FGP_TV
 
     rng = np.random.default_rng(sum(shape))
     x = rng.random(shape).astype(np.float32)
-    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0)):
-        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
-        a = FGP_TV(x, 0.05, 80, epsil, method, nonneg, device="gpu", infovector=ia)
+    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0), (0, 0, 1e-3)):
+        ib = np.zeros(2, np.float32)
         monkeypatch.setenv("CILREG_FGP_KERNEL", "simple")
         b = FGP_TV(x, 0.05, 80, epsil, method, nonneg, device="gpu", infovector=ib)
+        for kernel in (None, "stream"):
+            if kernel is None:
+                monkeypatch.delenv("CILREG_FGP_KERNEL")
+            else:
+                monkeypatch.setenv("CILREG_FGP_KERNEL", kernel)
+            ia = np.zeros(2, np.float32)
+            a = FGP_TV(x, 0.05, 80, epsil, method, nonneg, device="gpu", infovector=ia)
+            assert int(ia[0]) == int(ib[0])
+            assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
         monkeypatch.delenv("CILREG_FGP_KERNEL")
-        assert int(ia[0]) == int(ib[0])
-        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
 
 
 REPLAY_CALLS = {
@@ -327,8 +337,10 @@ def test_fgp_tensor_copy_staging_equals_thread_loads(shape, monkeypatch):
         monkeypatch.setenv("CILREG_FGP_TMA", "1")  # staging at any size (by default from 2^25 voxels)
         a = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ia)
         monkeypatch.setenv("CILREG_FGP_TMA", "0")
+        monkeypatch.setenv("CILREG_FGP_KERNEL", "stream")  # the one-voxel thread-loading kernel
         b = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ib)
         monkeypatch.delenv("CILREG_FGP_TMA")
+        monkeypatch.delenv("CILREG_FGP_KERNEL")
         assert int(ia[0]) == int(ib[0])
         np.testing.assert_array_equal(a, b)
 
@@ -369,7 +381,9 @@ def test_fgp_iteration_pairs_equal_single_iterations(shape, monkeypatch):
         monkeypatch.setenv("CILREG_FGP_PAIR", "1")
         a = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ia)
         monkeypatch.delenv("CILREG_FGP_PAIR")
+        monkeypatch.setenv("CILREG_FGP_KERNEL", "stream")  # single iterations of the same one-voxel arithmetic
         b = FGP_TV(x, 0.05, iters, epsil, method, nonneg, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_FGP_KERNEL")
         assert int(ia[0]) == int(ib[0])
         np.testing.assert_array_equal(a, b)
 
@@ -640,3 +654,39 @@ def test_rof_2d_persistent_launch_equals_one_launch_per_iteration(shape, monkeyp
         monkeypatch.delenv("CILREG_ROF_KERNEL")
         np.testing.assert_array_equal(a, b)
         np.testing.assert_array_equal(am, bm)
+
+
+def test_fgp_two_voxel_kernel_with_arrays_off_8_byte_alignment():
+    """The two-voxel FGP kernel with device arrays that start 4 bytes off an
+    8-byte boundary runs its 4-byte variant: the same iterates bit for bit."""
+    import ctypes
+    import os
+
+    import torch
+    from conftest import PKG
+
+    P = ctypes.POINTER(ctypes.c_float)
+    lib = ctypes.CDLL(os.path.join(PKG, "ccpi", "filters", "libcilregcuda.so"))
+    lib.cilreg_fgp_tv_dev.argtypes = [ctypes.c_void_p, ctypes.c_void_p, P, ctypes.c_float, ctypes.c_int,
+                                      ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_void_p]
+    lib.cilreg_fgp_tv_dev.restype = ctypes.c_int
+    lib.cilreg_last_error.restype = ctypes.c_char_p
+    shape = (24, 300, 298)  # 2,145,600 voxels: the two-voxel kernel's range
+    n = int(np.prod(shape))
+    x = np.random.default_rng(71).random(shape).astype(np.float32)
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for off in (0, 1):
+        buf_in = torch.zeros(n + 2, device="cuda")
+        buf_out = torch.zeros(n + 2, device="cuda")
+        buf_in[off:off + n] = torch.from_numpy(x.ravel()).cuda()
+        info = np.zeros(2, np.float32)
+        st = lib.cilreg_fgp_tv_dev(buf_in.data_ptr() + 4 * off, buf_out.data_ptr() + 4 * off, info.ctypes.data_as(P),
+                                   0.04, 45, 1e-4, 0, 1, shape[2], shape[1], shape[0], stream)
+        assert st == 0, lib.cilreg_last_error()
+        torch.cuda.synchronize()
+        outs.append((buf_out[off:off + n].cpu().numpy().reshape(shape), info.copy()))
+    (a, ia), (b, ib) = outs
+    assert int(ia[0]) == int(ib[0])
+    np.testing.assert_array_equal(a, b)
