@@ -2,11 +2,14 @@
 //
 // All volumes advance together, driven by a device-resident descriptor table
 // (dims, state pointers, lambda, stop control) and a tile -> volume map, and
-// every volume keeps its own stopping rule.  Two schedules:
+// every volume keeps its own stopping rule.  Three schedules:
 //   * graph: each iteration is ONE kernel launch (two for 2D TGV) over a flat
 //     grid of every volume's tiles, a finalize CTA per volume on check
 //     iterations; the whole loop is captured into one CUDA graph and launched
 //     once (CILREG_BATCH_GRAPH=0: plain launches);
+//   * graph of two-voxel launches (FGP, 3D volumes with even x extents and
+//     8-byte aligned arrays): the same with the tiles of k_fgp_x2_batch
+//     (fgp_x2.cu), two voxels per thread;
 //   * persistent (FGP): one launch runs every iteration of every volume; its
 //     CTAs take (iteration, tile) items from a device-side queue and wait
 //     only for their own volume's previous iteration (k_fgp_persistent,
@@ -16,7 +19,7 @@
 // candidate schedule and z chunk on the batch itself and keeps the fastest,
 // per GPU name and batch shape, in the process and in a cache file
 // (CILREG_AUTOTUNE_CACHE, default ~/.cache/cilreg-gb300/autotune.tsv; an
-// empty value keeps it in the process only).  CILREG_BATCH_MODE=graph or
+// empty value keeps it in the process only).  CILREG_BATCH_MODE=graph, x2 or
 // persistent fixes the schedule ("persistent:<MB>" with volume groups of at
 // most that many MB of state).
 #include <math.h>
@@ -159,12 +162,14 @@ struct FgpBatch {
     size_t ring_bytes = 0;
     long long ntiles = 0;
     bool wide = false;  // some volume has 2^31 voxels or more
+    bool x2 = false;    // two-voxel tiles (k_fgp_x2_batch)
 };
 
 int fgp_build(FgpBatch& B, Scratch& sc, const BatchLayout& L, const float* const* f, float* const* u,
-              const float* lams, int zc_override, cudaStream_t s) {
+              const float* lams, int zc_override, cudaStream_t s, bool x2 = false) {
     const int nvol = (int)L.dims.size();
     const int nc = L.three ? 3 : 2;
+    B.x2 = x2;
     B.vols.assign(nvol, FgpBatchVol());
     B.ntiles = 0;
     size_t ring_floats = 0;
@@ -174,7 +179,10 @@ int fgp_build(FgpBatch& B, Scratch& sc, const BatchLayout& L, const float* const
         V.d = d;
         if (d.n >= (1LL << 31)) B.wide = true;
         V.zc = zc_override > 0 ? (d.nz > 1 ? (zc_override < d.nz ? zc_override : d.nz) : 1) : fgp_default_zchunk(d);
-        fgp_tile_grid(d, V.zc, V.gx, V.gy, V.gz);
+        if (x2)
+            fgp_x2_tile_grid(d, V.zc, V.gx, V.gy, V.gz);
+        else
+            fgp_tile_grid(d, V.zc, V.gx, V.gy, V.gz);
         V.tile_base = B.ntiles;
         B.ntiles += (long long)V.gx * V.gy * V.gz;
         ring_floats += align256(sizeof(float) * (size_t)d.n) / sizeof(float) * 3 * nc;
@@ -238,8 +246,12 @@ int fgp_enqueue(FgpBatch& B, int nvol, bool three, int iters, float epsil, int m
         const int check = (checking && it % 5 == 0) ? 1 : 0;
         const int write_u = (it == iters - 1) || check || (checking && (it + 1) % 5 == 0);
         const int write_p = (it != iters - 1);
-        CILREG_TRY(fgp_batch_step(B.d_vols, B.d_tile_vol, B.ntiles, three, B.wide, it, cprev, nonneg == 1, methodTV != 0,
-                                  write_u, write_p, check, s));
+        if (B.x2)
+            CILREG_TRY(fgp_x2_batch_step(B.d_vols, B.d_tile_vol, B.ntiles, it, cprev, nonneg == 1, methodTV != 0,
+                                         write_u, write_p, check, s));
+        else
+            CILREG_TRY(fgp_batch_step(B.d_vols, B.d_tile_vol, B.ntiles, three, B.wide, it, cprev, nonneg == 1,
+                                      methodTV != 0, write_u, write_p, check, s));
         note_launch();
         const float tkp1 = (1.0f + sqrtf(1.0f + 4.0f * tk * tk)) * 0.5f;  // FGP_TV_core.c:138
         cprev = (tk - 1.0f) / tkp1;
@@ -371,7 +383,7 @@ int fgp_persistent_enqueue(FgpBatch& B, const BatchLayout& L, int it0, int nits,
 
 // schedule of a batched FGP run; code = mode * 100000 + group_mb * 100 + zc
 struct FgpSchedule {
-    int mode = 0;      // 0 graph of flat-grid launches, 1 persistent kernel
+    int mode = 0;      // 0 graph of flat-grid launches, 1 persistent kernel, 2 graph of two-voxel launches
     int zc = 0;        // z chunk of the streaming tiles (0: fgp_default_zchunk)
     int group_mb = 0;  // persistent: L2 groups of at most this many MB of state (0: one group)
     int code() const { return mode * 100000 + group_mb * 100 + zc; }
@@ -392,7 +404,10 @@ int fgp_run_schedule(const FgpSchedule& S, const BatchLayout& L, const float* co
     const int nvol = (int)L.dims.size();
     Scratch sc(s);
     FgpBatch B;
-    CILREG_TRY(fgp_build(B, sc, L, f, u, lams, S.zc, s));
+    const bool x2 = S.mode == 2;
+    if (x2 && !fgp_x2_batch_usable(L.dims.data(), f, u, nvol))
+        return fail(ERR_ARG, __FILE__, __LINE__, "two-voxel batch: a volume is 2D, has an odd x extent or misaligned arrays");
+    CILREG_TRY(fgp_build(B, sc, L, f, u, lams, S.zc, s, x2));
     CILREG_TRY(fgp_reset(B, nvol, iters, s));
     if (S.mode == 1 && iters > 0)
         CILREG_TRY(fgp_persistent_enqueue(B, L, 0, iters, iters, epsil, methodTV, nonneg, S.group_mb, kWaitLimit, s,
@@ -410,10 +425,13 @@ int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* cons
                         int methodTV, int nonneg, cudaStream_t s, FgpSchedule& out) {
     out = FgpSchedule();
     if (const char* m = getenv("CILREG_BATCH_MODE")) {
-        // "graph", "persistent" or "persistent:<MB>" (volume groups of at most MB of state)
+        // "graph", "x2" (graph of two-voxel launches), "persistent" or
+        // "persistent:<MB>" (volume groups of at most MB of state)
         if (m[0] == 'p') {
             out.mode = 1;
             if (const char* c = strchr(m, ':')) out.group_mb = atoi(c + 1) < 0 ? 0 : atoi(c + 1) % 1000;
+        } else if (m[0] == 'x' && fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size())) {
+            out.mode = 2;
         }
         return OK;
     }
@@ -422,10 +440,13 @@ int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* cons
     const int c = cached_choice(key);
     if (c != 0) {
         out = FgpSchedule::from(c);
+        // the cache key holds the extents only: this call's arrays may not suit two-voxel tiles
+        if (out.mode == 2 && !fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size())) out.mode = 0;
         return OK;
     }
     std::vector<FgpSchedule> cand;
-    for (int mode = 0; mode < 2; mode++)
+    const int modes = fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size()) ? 3 : 2;
+    for (int mode = 0; mode < modes; mode++)
         for (int zc : {64, 32, 16}) {
             FgpSchedule t;
             t.mode = mode;

@@ -50,20 +50,19 @@ struct X2Args {
     int coff;
 };
 
+// One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk and
+// returns its threads' FP32 sums of the stopping check (CHECK).
 template <bool CHECK, bool ALIGNED>
-__global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, const StopCtl* ctl,
-                                                   double2* partials) {
+__device__ __forceinline__ void x2_tile(const X2Args& a, const Dims& d, int zc, int bx, int by, int bz,
+                                        float& pa_out, float& pb_out) {
     __shared__ __align__(16) float sR1[ROWS * TW];
     __shared__ __align__(16) float sR2[ROWS * TW];
     __shared__ __align__(16) float sU[2][ROWS * TW];
-    pdl_wait();  // the previous iteration has completed (launch_pdl)
-    pdl_trigger();
-    if (ctl->stop) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny, nz = d.nz;
-    const int X = tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first voxel
-    const int y = blockIdx.y * OYP - 1 + ty;
-    const int z0 = blockIdx.z * zc;
+    const int X = tile_x0(bx) + 2 * tx;  // x of the pair's first voxel
+    const int y = by * OYP - 1 + ty;
+    const int z0 = bz * zc;
     const int z1 = min(z0 + zc, nz);
     // both voxels lie in the volume or neither does (nx even, X even)
     const bool in_xy = X >= 0 && X < nx && y >= 0 && y < ny;
@@ -178,7 +177,63 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, con
         up = u;
         uo = uo_next;
     }
-    if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
+    pa_out = pa.x + pa.y;
+    pb_out = pb.x + pb.y;
+}
+
+template <bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, const StopCtl* ctl,
+                                                   double2* partials) {
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    float pa = 0.f, pb = 0.f;
+    x2_tile<CHECK, ALIGNED>(a, d, zc, blockIdx.x, blockIdx.y, blockIdx.z, pa, pb);
+    if (CHECK) block_pair_partial<NTP>(pa, pb, partials, block_slot());
+}
+
+// one iteration `it` of every volume of a batch (8-byte aligned arrays): a
+// flat grid over all volumes' tiles, P^j in ring[j mod 3] as in
+// k_fgp_stream_batch
+template <bool CHECK>
+__global__ void __launch_bounds__(NTP, 4) k_fgp_x2_batch(const FgpBatchVol* __restrict__ vols,
+                                                         const int* __restrict__ tile_vol, int it, float c,
+                                                         int nonneg, int aniso, int write_u, int write_p) {
+    const long long t = blockIdx.x;
+    const FgpBatchVol& V = vols[tile_vol[t]];
+    if (V.ctl->stop) return;
+    const long long lt = t - V.tile_base;
+    const int bx = (int)(lt % V.gx);
+    const int by = (int)((lt / V.gx) % V.gy);
+    const int bz = (int)(lt / ((long long)V.gx * V.gy));
+    // the volume's arguments in shared memory: their uses read them there
+    // instead of holding eleven pointers in registers
+    __shared__ X2Args a;
+    __shared__ Dims d;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        for (int q = 0; q < 3; q++) {
+            a.pn[q] = V.ring[it % 3][q];
+            a.pc[q] = V.ring[(it + 2) % 3][q];
+            a.po[q] = V.ring[(it + 1) % 3][q];
+        }
+        a.f = V.f;
+        a.u = V.u;
+        a.lam = V.lam;
+        a.c = c;
+        a.multip = V.multip;
+        a.nonneg = nonneg;
+        a.aniso = aniso;
+        a.write_u = write_u;
+        a.write_p = write_p;
+        a.carr = nullptr;
+        a.cbase = nullptr;
+        a.coff = 0;
+        d = V.d;
+    }
+    __syncthreads();
+    float pa = 0.f, pb = 0.f;
+    x2_tile<CHECK, true>(a, d, V.zc, bx, by, bz, pa, pb);
+    if (CHECK) block_pair_partial<NTP>(pa, pb, V.partials, lt);
 }
 
 using X2Kernel = decltype(&k_fgp_x2<false, true>);
@@ -189,6 +244,32 @@ X2Kernel pick(bool check, bool aligned) {
 }
 
 }  // namespace
+
+bool fgp_x2_batch_usable(const Dims* dims, const float* const* f, float* const* u, int nvol) {
+    for (int v = 0; v < nvol; v++)
+        if (dims[v].nz < 2 || dims[v].nx % 2 != 0 || dims[v].n >= (1LL << 31) || !host_aligned8(f[v]) ||
+            !host_aligned8(u[v]))
+            return false;
+    return nvol > 0;
+}
+
+void fgp_x2_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz) {
+    gx = tiles_x(d.nx);
+    gy = (d.ny + OYP - 1) / OYP;
+    gz = (d.nz + zc - 1) / zc;
+}
+
+int fgp_x2_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, int it, float c,
+                      int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s) {
+    if (ntiles < 1 || ntiles > 2147483647LL) return fail(ERR_ARG, __FILE__, __LINE__, "tile count %lld", ntiles);
+    const dim3 grid((unsigned)ntiles), block(PX, ROWS, 1);
+    if (check)
+        k_fgp_x2_batch<true><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p);
+    else
+        k_fgp_x2_batch<false><<<grid, block, 0, s>>>(d_vols, d_tile_vol, it, c, nonneg, aniso, write_u, write_p);
+    CILREG_CUDA(cudaGetLastError());
+    return OK;
+}
 
 TiledPlan fgp_x2_plan(const Dims& d) {
     TiledPlan T;

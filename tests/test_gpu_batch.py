@@ -141,6 +141,43 @@ def test_fgp_persistent_batch_on_the_seeded_batch_equals_graph(monkeypatch):
             assert torch.equal(a, b), mode
 
 
+@pytest.mark.parametrize("epsil", [0.0, 3e-4])
+def test_fgp_two_voxel_batch_equals_one_voxel_batch(epsil, monkeypatch):
+    """Every x extent even: the graph of two-voxel launches agrees with the
+    graph of one-voxel launches to the last bits (the paired instructions
+    round each product and sum once, as the one-voxel code does) and stops
+    at the same iterations."""
+    from ccpi.filters.batch import FGP_TV_batch
+
+    vols = _volumes(SHAPES_3D_X4, 10)
+    lams = [0.03 + 0.01 * i for i in range(len(vols))]
+    runs = {}
+    for mode in ("graph", "x2"):
+        monkeypatch.setenv("CILREG_BATCH_MODE", mode)
+        infos = np.zeros((len(vols), 2), np.float32)
+        runs[mode] = (FGP_TV_batch(vols, lams, 60, epsil, 0, 1, infovectors=infos), infos)
+    (ref, ref_info), (got, got_info) = runs["graph"], runs["x2"]
+    np.testing.assert_array_equal(got_info[:, 0], ref_info[:, 0])
+    for a, b in zip(got, ref):
+        assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-5)
+
+
+def test_fgp_two_voxel_batch_equals_single_calls(monkeypatch):
+    """Volumes of 2^21 voxels and more, where a single call runs the
+    two-voxel kernel too: the batch gives its results bit for bit, whatever
+    the z chunks of the two runs."""
+    import torch
+    from ccpi.filters.batch import FGP_TV_batch
+    from ccpi.filters.regularisers import FGP_TV
+
+    vols = [torch.from_numpy(v).cuda() for v in _volumes([(40, 231, 230), (33, 250, 258)], 11)]
+    monkeypatch.setenv("CILREG_BATCH_MODE", "x2")
+    got = FGP_TV_batch(vols, [0.03, 0.05], 30, 0.0, 0, 1)
+    for v, lam, o in zip(vols, (0.03, 0.05), got):
+        ref = FGP_TV(v.cpu().numpy(), lam, 30, 0.0, 0, 1, device="gpu")
+        np.testing.assert_array_equal(o.cpu().numpy(), ref)
+
+
 def test_batch_rejects_mixed_dimensionality():
     from ccpi.filters.batch import FGP_TV_batch
 
