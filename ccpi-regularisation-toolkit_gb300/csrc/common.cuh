@@ -54,6 +54,15 @@ __device__ __forceinline__ float ldg(const float* p, long long v) { return __ldg
 
 __device__ __forceinline__ float sgnf(float x) { return (float)((x > 0.0f) - (x < 0.0f)); }
 
+// p / max(|p|, 1), the anisotropic projection of FGP and PD (utils.c:198-210),
+// with the IEEE quotient's value and no division: p itself for |p| <= 1, the
+// exact quotient +-1 for finite |p| > 1, NaN for an infinite p (and p - p is
+// NaN for a NaN p too)
+__device__ __forceinline__ float unit_clip(float p) {
+    const float a = fabsf(p);
+    return (a <= 1.0f) ? p : ((a <= 3.4028234664e38f) ? copysignf(1.0f, p) : p - p);
+}
+
 // flags between CTAs of one launch: an acquire load and a release store at
 // GPU scope
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {

@@ -17,6 +17,11 @@
 // the first plane and W(k+1) at the last one are selects: W formed from
 // mirrored planes equals the mirrored W only up to rounding.
 //
+// The two reciprocals of W (1/den and the diffusivity 1/(1 + den/sigma^2))
+// are rcp2's (pair.cuh): the approximate reciprocal with one paired
+// Newton-Raphson step, within an ulp of the IEEE reciprocal of the one-voxel
+// kernels and much cheaper to issue (0.823 -> 0.707 ms per 512^3 iteration).
+//
 // A CTA of 16 x ROWS threads holds a 32 x ROWS tile with a two-voxel halo:
 // W on the inner 30 x (ROWS-2) points, the update on the inner 28 x (ROWS-4),
 // whole pairs (threads 1..14 of rows 2..ROWS-3).  Tile x origins are even
@@ -150,11 +155,10 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
             nn = add2(add2(add2(nn, xy2), xz2), yz2);
             float2 oo = fma2(add2(gx2, gy2), gzz, fma2(add2(gx2, gz2), gyy, mul2(add2(gy2, gz2), gxx)));
             oo = sub2(sub2(sub2(oo, xy2), xz2), yz2);
-            const float2 iq = make_float2(__frcp_rn((den.x <= EPS) ? EPS : den.x),
-                                          __frcp_rn((den.y <= EPS) ? EPS : den.y));
+            const float2 iq = rcp2(make_float2((den.x <= EPS) ? EPS : den.x, (den.y <= EPS) ? EPS : den.y));
             const float2 vn = mul2(nn, iq), vo = mul2(oo, iq);
             const float2 q = fma2(den, isg22, ONE2);
-            const float2 c = make_float2(__frcp_rn(q.x), __frcp_rn(q.y));
+            const float2 c = rcp2(q);
             wc = wb;
             wb = wa;
             wa = fma2(mul2(c, c), vn, mul2(c, vo));

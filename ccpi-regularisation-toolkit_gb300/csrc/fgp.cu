@@ -95,9 +95,9 @@ __global__ void __launch_bounds__(256) k_fgp_step(FgpArgs a, Dims d, int kz, con
                         p3 = p3 * sq;
                     }
                 } else {
-                    p1 = p1 / fmaxf(fabsf(p1), 1.0f);
-                    p2 = p2 / fmaxf(fabsf(p2), 1.0f);
-                    p3 = p3 / fmaxf(fabsf(p3), 1.0f);
+                    p1 = unit_clip(p1);
+                    p2 = unit_clip(p2);
+                    p3 = unit_clip(p3);
                 }
                 a.pn[0][v] = p1;
                 a.pn[1][v] = p2;

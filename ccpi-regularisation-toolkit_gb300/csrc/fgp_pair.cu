@@ -86,9 +86,9 @@ __device__ __forceinline__ void p_update(float r1, float r2, float r3, float g1,
         p2 = p2 * sq;
         p3 = p3 * sq;
     } else {
-        p1 = p1 / fmaxf(fabsf(p1), 1.f);
-        p2 = p2 / fmaxf(fabsf(p2), 1.f);
-        p3 = p3 / fmaxf(fabsf(p3), 1.f);
+        p1 = unit_clip(p1);
+        p2 = unit_clip(p2);
+        p3 = unit_clip(p3);
     }
 }
 

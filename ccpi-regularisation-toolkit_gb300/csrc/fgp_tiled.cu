@@ -183,9 +183,9 @@ __device__ __forceinline__ void fgp_stream_tile(const TiledArgs& a, const Dims& 
                     p2 = p2 * sq;
                     p3 = p3 * sq;
                 } else {
-                    p1 = p1 / fmaxf(fabsf(p1), 1.f);
-                    p2 = p2 / fmaxf(fabsf(p2), 1.f);
-                    p3 = p3 / fmaxf(fabsf(p3), 1.f);
+                    p1 = unit_clip(p1);
+                    p2 = unit_clip(p2);
+                    p3 = unit_clip(p3);
                 }
                 a.pn[0][v] = p1;
                 a.pn[1][v] = p2;

@@ -161,10 +161,9 @@ __device__ __forceinline__ void x2_tile(const X2Args& a, const Dims& d, int zc, 
                     p2 = mul2(p2, sq);
                     p3 = mul2(p3, sq);
                 } else {
-                    auto an = [](float p) { return p / fmaxf(fabsf(p), 1.f); };
-                    p1 = make_float2(an(p1.x), an(p1.y));
-                    p2 = make_float2(an(p2.x), an(p2.y));
-                    p3 = make_float2(an(p3.x), an(p3.y));
+                    p1 = make_float2(unit_clip(p1.x), unit_clip(p1.y));
+                    p2 = make_float2(unit_clip(p2.x), unit_clip(p2.y));
+                    p3 = make_float2(unit_clip(p3.x), unit_clip(p3.y));
                 }
                 store_pair<ALIGNED>(a.pn[0] + v, p1, vx, vy);
                 store_pair<ALIGNED>(a.pn[1] + v, p2, vx, vy);

@@ -49,10 +49,18 @@ __device__ __forceinline__ float2 normalise2(float2 dp, float2 s) {
     return mul2(dp, make_float2(rsqrtf(s.x), rsqrtf(s.y)));
 }
 
-// second difference over its magnitude, per component (llt_term of llt.cu)
-__device__ __forceinline__ float2 llt_term2(float2 v) {
-    return make_float2(v.x / (fabsf(v.x) + 1.0e-12f), v.y / (fabsf(v.y) + 1.0e-12f));
+// v / (|v| + 1e-12), the second difference over its magnitude (llt_term
+// of llt.cu), with the IEEE quotient's value and without its division for
+// almost every v: from |v| = 2^-15 on, 1e-12 is below half an ulp of |v|, so
+// the rounded denominator is |v| and the quotient exactly +-1; v = +-0 gives
+// itself.  Only the other values (below 2^-15, infinite, NaN) divide.
+__device__ __forceinline__ float llt_term1(float v) {
+    const float a = fabsf(v);
+    float r = (a == 0.0f) ? v : copysignf(1.0f, v);
+    if (!(a >= 0x1p-15f && a <= 3.4028234664e38f) && a != 0.0f) r = v / (a + 1.0e-12f);
+    return r;
 }
+__device__ __forceinline__ float2 llt_term2(float2 v) { return make_float2(llt_term1(v.x), llt_term1(v.y)); }
 
 template <bool CHECK, bool ALIGNED, int MINB>
 __global__ void __launch_bounds__(NTP, MINB)
@@ -203,8 +211,10 @@ __global__ void __launch_bounds__(NTP, MINB)
     if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
 }
 
-// four CTAs per SM at 64 registers (small spills): 0.933 ms per 512^3
-// iteration, against 0.996 ms for three CTAs at 80 registers without spills
+// four CTAs per SM at 64 registers (small spills): 0.879 ms per 512^3
+// iteration; a 16 x 32 CTA, two per SM, ran 0.882 ms, and three CTAs at 80
+// registers without spills 0.996 ms (against 0.933 ms, both before the sign
+// shortcut of llt_term1)
 constexpr int MINB = 4;
 using PairKernel = decltype(&k_llt_pair<false, true, MINB>);
 

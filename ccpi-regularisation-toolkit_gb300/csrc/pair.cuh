@@ -36,6 +36,16 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// 1/x per component, for normal x whose reciprocal is normal: the hardware's
+// approximate reciprocal (PTX rcp.approx.ftz.f32) refined by one
+// Newton-Raphson step r + r (1 - x r), whose error term is formed exactly by
+// the fused multiply-add; the step issues paired.
+__device__ __forceinline__ float2 rcp2(float2 x) {
+    float2 r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.x) : "f"(x.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.y) : "f"(x.y));
+    return fma2(r, fma2(neg2(x), r, make_float2(1.0f, 1.0f)), r);
+}
 
 // 8-byte access of a pair (shared or global memory, 8-byte aligned)
 __device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }

@@ -12,6 +12,8 @@
 
 #include <cuda_runtime.h>
 
+#include "common.cuh"
+
 namespace cilreg {
 
 // The reference's  (float)((double)num / D)  with D = 1.0 + lt a double:
@@ -61,7 +63,7 @@ __device__ __forceinline__ void pd_project_iso(float& p1, float& p2, float& p3) 
 }
 
 // anisotropic projection: each component over max(|P_c|, 1)  (utils.c:198-210)
-__device__ __forceinline__ float pd_project_aniso(float p) { return __fdiv_rn(p, fmaxf(fabsf(p), 1.0f)); }
+__device__ __forceinline__ float pd_project_aniso(float p) { return unit_clip(p); }
 
 // U = (U - tau div + lt f) / (1.0 + lt)  (PD_TV_core.c:249)
 __device__ __forceinline__ float pd_primal(float u, float tau, float dv, float lt, float f, const DoubleDivisor& D) {

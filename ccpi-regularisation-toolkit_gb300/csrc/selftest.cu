@@ -7,6 +7,7 @@
 // it with the same helper the kernels use, and writes whether the wait gave
 // up.  The host reads that status and checks that the context still runs
 // work afterwards.
+#include "pair.cuh"
 #include "runtime.cuh"
 #include "tma_ring.cuh"
 
@@ -29,6 +30,20 @@ __global__ void k_wait_limit_probe(int* out) {
 }
 
 __global__ void k_set_int(int* p, int v) { *p = v; }
+
+// rcp2 (pair.cuh) and CUDA's IEEE reciprocal of every x
+__global__ void k_reciprocal_probe(const float* x, float* approx, float* ieee, long long n) {
+    const long long i = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    const float a = x[i], b = (i + 1 < n) ? x[i + 1] : 1.0f;
+    const float2 r = pair::rcp2(make_float2(a, b));
+    approx[i] = r.x;
+    ieee[i] = __frcp_rn(a);
+    if (i + 1 < n) {
+        approx[i + 1] = r.y;
+        ieee[i + 1] = __frcp_rn(b);
+    }
+}
 
 }  // namespace
 }  // namespace cilreg
@@ -57,5 +72,25 @@ extern "C" int cilreg_selftest_wait_limit(int gpu_device, int* ran_out) {
     CILREG_CUDA(cudaStreamSynchronize(s));
     if (after != 7) return fail(ERR_CUDA, __FILE__, __LINE__, "no work ran after the wait probe");
     *ran_out = (h == 2) ? 1 : 0;
+    return OK;
+}
+
+extern "C" int cilreg_selftest_reciprocal(int gpu_device, const float* x, float* approx, float* ieee,
+                                          long long n) {
+    using namespace cilreg;
+    if (!x || !approx || !ieee || n < 1 || n > (1LL << 30))
+        return fail(ERR_ARG, __FILE__, __LINE__, "bad reciprocal probe arguments (n = %lld)", n);
+    CILREG_TRY(use_device(gpu_device));
+    cudaStream_t s = thread_stream(gpu_device);
+    Scratch sc(s);
+    float* d = sc.floats(3 * n);
+    if (!d) return sc.status();
+    CILREG_CUDA(cudaMemcpyAsync(d, x, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    const long long pairs = (n + 1) / 2;
+    k_reciprocal_probe<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(d, d + n, d + 2 * n, n);
+    CILREG_CUDA(cudaGetLastError());
+    CILREG_CUDA(cudaMemcpyAsync(approx, d + n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CILREG_CUDA(cudaMemcpyAsync(ieee, d + 2 * n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CILREG_CUDA(cudaStreamSynchronize(s));
     return OK;
 }

@@ -304,6 +304,12 @@ int cilreg_selftest_wait_limit(int gpu_device, int *ran_out);
  * the call reported it, and the device then still ran work.  0 or a
  * negative status. */
 int cilreg_selftest_batch_wait(int gpu_device, int *ran_out);
+/* Self-test of the kernels' reciprocal (the approximate reciprocal with one
+ * Newton-Raphson step, used by the two-voxel fourth-order diffusion kernel):
+ * approx[i] = that reciprocal of the host array x[i], ieee[i] = CUDA's
+ * correctly rounded reciprocal of x[i], for 1 <= n <= 2^30.  0 or a negative
+ * status. */
+int cilreg_selftest_reciprocal(int gpu_device, const float *x, float *approx, float *ieee, long long n);
 
 #ifdef __cplusplus
 }

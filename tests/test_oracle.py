@@ -171,3 +171,36 @@ def test_rof_fp64_unrolled_oracle_matches_port(shape):
         y = R64.rof_unrolled(torch.tensor(f, dtype=torch.float64), torch.tensor(0.05, dtype=torch.float64), iters,
                              0.01).numpy()
         assert np.max(np.abs(y - ref)) <= rel_tol(ref, 1e-5)
+
+
+def test_llt_term_is_a_sign_copy_from_two_to_the_minus_15():
+    """The two-voxel LLT-ROF kernel takes v / (|v| + 1e-12) as +-1 for
+    |v| >= 2^-15 and as v for v = +-0, dividing only otherwise: in FP32 the
+    IEEE quotient has exactly those values, and just below 2^-15 it does not."""
+    rng = np.random.default_rng(13)
+    e = rng.uniform(-15, 127, 3_000_000)
+    v = (np.where(rng.random(e.size) < 0.5, -1.0, 1.0) * 2.0 ** e).astype(np.float32)
+    v = v[np.isfinite(v) & (np.abs(v) >= np.float32(2.0 ** -15))]
+    eps = np.float32(1e-12)
+    with np.errstate(over="ignore"):
+        np.testing.assert_array_equal(v / (np.abs(v) + eps), np.sign(v))
+    z = np.float32([0.0, -0.0])
+    q = z / (np.abs(z) + eps)
+    np.testing.assert_array_equal(np.signbit(q), np.signbit(z))
+    below = np.nextafter(np.float32(2.0 ** -15), np.float32(0))
+    assert below / (below + eps) != np.float32(1.0)
+
+
+def test_anisotropic_projection_is_a_clip_without_division():
+    """The kernels take p / max(|p|, 1) as p for |p| <= 1 and as +-1 beyond:
+    in FP32 the IEEE quotient has exactly those values."""
+    rng = np.random.default_rng(14)
+    e = rng.uniform(-40, 127, 3_000_000)
+    p = (np.where(rng.random(e.size) < 0.5, -1.0, 1.0) * 2.0 ** e).astype(np.float32)
+    p = np.concatenate([p[np.isfinite(p)], np.float32([0.0, -0.0, 1.0, -1.0]),
+                        np.nextafter(np.float32([1.0, -1.0]), np.float32(0)),
+                        np.nextafter(np.float32([1.0, -1.0]), np.float32([2.0, -2.0]))])
+    q = p / np.maximum(np.abs(p), np.float32(1.0))
+    clip = np.where(np.abs(p) <= 1, p, np.sign(p)).astype(np.float32)
+    np.testing.assert_array_equal(q, clip)
+    np.testing.assert_array_equal(np.signbit(q), np.signbit(clip))
