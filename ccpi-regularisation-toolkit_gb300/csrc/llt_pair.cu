@@ -53,14 +53,19 @@ __device__ __forceinline__ float2 normalise2(float2 dp, float2 s) {
 // of llt.cu), with the IEEE quotient's value and without its division for
 // almost every v: from |v| = 2^-15 on, 1e-12 is below half an ulp of |v|, so
 // the rounded denominator is |v| and the quotient exactly +-1; v = +-0 gives
-// itself.  Only the other values (below 2^-15, infinite, NaN) divide.
-__device__ __forceinline__ float llt_term1(float v) {
+// itself.  Only the other values (below 2^-15, infinite, NaN) divide: a step
+// forms the six terms of its pair by sign copies and, when any of them needs
+// it, all six by the division (one branch).
+__device__ __forceinline__ float llt_sign1(float v) { return (v == 0.0f) ? v : copysignf(1.0f, v); }
+__device__ __forceinline__ float2 llt_sign2(float2 v) { return make_float2(llt_sign1(v.x), llt_sign1(v.y)); }
+__device__ __forceinline__ bool llt_divides(float v) {
     const float a = fabsf(v);
-    float r = (a == 0.0f) ? v : copysignf(1.0f, v);
-    if (!(a >= 0x1p-15f && a <= 3.4028234664e38f) && a != 0.0f) r = v / (a + 1.0e-12f);
-    return r;
+    return !(a >= 0x1p-15f && a <= 3.4028234664e38f) && a != 0.0f;
 }
-__device__ __forceinline__ float2 llt_term2(float2 v) { return make_float2(llt_term1(v.x), llt_term1(v.y)); }
+__device__ __forceinline__ bool llt_divides2(float2 v) { return llt_divides(v.x) | llt_divides(v.y); }
+__device__ __forceinline__ float2 llt_quot2(float2 v) {
+    return make_float2(v.x / (fabsf(v.x) + 1.0e-12f), v.y / (fabsf(v.y) + 1.0e-12f));
+}
 
 template <bool CHECK, bool ALIGNED, int MINB>
 __global__ void __launch_bounds__(NTP, MINB)
@@ -141,16 +146,25 @@ __global__ void __launch_bounds__(NTP, MINB)
             const float2 n1 = normalise2(yp, add2(add2(fma2(yp, yp, mx2), mz2), EPS2));
             const float2 n2 = normalise2(xp, add2(add2(fma2(xp, xp, my2), mz2), EPS2));
             const float2 n3 = normalise2(zp, add2(add2(fma2(zp, zp, my2), mx2), EPS2));
+            const float2 v3 = add2(fma2(MTWO2, c, uhi), ulo);
+            const float2 v1 = add2(fma2(MTWO2, c, ch), cl);
+            const float2 v2 = add2(fma2(MTWO2, c, uyh), uyl);
+            float2 t3 = llt_sign2(v3), t1 = llt_sign2(v1), t2 = llt_sign2(v2);
+            if (llt_divides2(v3) | llt_divides2(v1) | llt_divides2(v2)) {
+                t3 = llt_quot2(v3);
+                t1 = llt_quot2(v1);
+                t2 = llt_quot2(v2);
+            }
             l3c = l3b;
             l3b = l3a;
-            l3a = llt_term2(add2(fma2(MTWO2, c, uhi), ulo));
+            l3a = t3;
             r3c = r3b;
             r3b = r3a;
             r3a = n3;
             st2(sR1[WM] + o, n1);
             st2(sR2[WM] + o, n2);
-            st2(sL1[WM] + o, llt_term2(add2(fma2(MTWO2, c, ch), cl)));
-            st2(sL2[WM] + o, llt_term2(add2(fma2(MTWO2, c, uyh), uyl)));
+            st2(sL1[WM] + o, t1);
+            st2(sL2[WM] + o, t2);
         }
         // C. update plane kf = j-2 (LLT_ROF_core.c:404-436); its terms were
         // published in the previous step

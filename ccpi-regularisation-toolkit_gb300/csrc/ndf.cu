@@ -86,8 +86,12 @@ int ndf_run(const float* f, float* u_out, float lam, float sigma, int iters, flo
     if (!linear && (penalty < 1 || penalty > 5))
         return fail(ERR_ARG, __FILE__, __LINE__, "No penalty function selected! Use 1,2,3,4 or 5.");
     const int pen = linear ? 0 : penalty;
-    const float sg = (float)((double)sigma / sqrt(2.0));  // Diffusion_core.c:57
-    const float isg = linear ? 0.0f : 1.0f / sg;
+    const float sg_ref = (float)((double)sigma / sqrt(2.0));  // Diffusion_core.c:57
+    const float isg = linear ? 0.0f : 1.0f / sg_ref;
+    // the kernels compare |e| with sg only; below 0 every such comparison
+    // gives what it gives at 0 up to the sign of a zero flux, and from 0 on a
+    // flux whose sign is taken has e != 0 (flux in ndf_tiled.cuh)
+    const float sg = fmaxf(sg_ref, 0.0f);
     const bool three = d.nz > 1;
     Scratch scratch(s);
     const Launch3 L = plan_launch(d);

@@ -50,7 +50,8 @@ __device__ __forceinline__ float2 flux2(float2 e, float sg, float2 isg2) {
     if (PEN == 0) return e;
     if (PEN == 1) {
         const float2 r = mul2(e, isg2);
-        return make_float2((fabsf(e.x) > sg) ? sgnf(e.x) : r.x, (fabsf(e.y) > sg) ? sgnf(e.y) : r.y);
+        return make_float2((fabsf(e.x) > sg) ? copysignf(1.0f, e.x) : r.x,
+                           (fabsf(e.y) > sg) ? copysignf(1.0f, e.y) : r.y);
     }
     if (PEN == 2) {
         const float2 r = mul2(e, isg2);
@@ -67,7 +68,7 @@ __device__ __forceinline__ float2 flux2(float2 e, float sg, float2 isg2) {
     // PEN == 5
     const float2 r = mul2(e, isg2);
     auto one = [&](float ev, float rv) {
-        if (fabsf(ev) <= 2.0f * sg) return (fabsf(ev) > sg) ? sgnf(ev) : rv;
+        if (fabsf(ev) <= 2.0f * sg) return (fabsf(ev) > sg) ? copysignf(1.0f, ev) : rv;
         return 0.0f;
     };
     return make_float2(one(e.x, r.x), one(e.y, r.y));

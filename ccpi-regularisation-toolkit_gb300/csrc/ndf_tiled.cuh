@@ -13,7 +13,7 @@ namespace cilreg {
 template <int PEN>
 __device__ __forceinline__ float flux(float e, float sg, float isg) {
     if (PEN == 0) return e;  // linear diffusion (sigma == 0)
-    if (PEN == 1) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
+    if (PEN == 1) return (fabsf(e) > sg) ? copysignf(1.0f, e) : e * isg;
     if (PEN == 2) {
         const float r = e * isg;
         return e * __frcp_rn(1.0f + r * r);
@@ -28,12 +28,14 @@ __device__ __forceinline__ float flux(float e, float sg, float isg) {
     }
     if (PEN == 4) return (fabsf(e) > sg) ? 0.0f : e;
     // PEN == 5
-    if (fabsf(e) <= 2.0f * sg) return (fabsf(e) > sg) ? sgnf(e) : e * isg;
+    if (fabsf(e) <= 2.0f * sg) return (fabsf(e) > sg) ? copysignf(1.0f, e) : e * isg;
     return 0.0f;
 }
 
+// sg >= 0 (the host clamps it), so |e| > sg means e != 0 and the sign of e is
+// a sign copy (the reference's sign function, which is 0 only at e == 0).
 // Every penalty is odd (flux(-e) == -flux(e) bit for bit: the sign enters
-// only through e itself or sgnf(e)), so the flux through a face can be formed
+// only through e itself or its sign copy), so the flux through a face can be formed
 // once and used with opposite signs by the two voxels that share it.
 
 struct NdfPlan {
