@@ -215,6 +215,93 @@ __global__ void __launch_bounds__(Geo<ROWS>::NTP, Geo<ROWS>::MINB)
     if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
 }
 
+// One 2D iteration (nz == 1), two pixels per thread: the pair of a 16 x 16
+// CTA is loaded once, W is formed on the inner 30 x 14 pixels into shared
+// memory, the update on the inner 28 x 12 (Diffus4th_order_core.c:103-150,
+// 237-265).  Two barriers, no plane loop: 256-thread CTAs, several per SM,
+// keep a 2D image's short launch latency-tolerant.
+constexpr int ROWS2 = 16;
+constexpr int NTP2 = PX * ROWS2, TP2 = TW * ROWS2, OY2 = ROWS2 - 4;
+
+template <bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP2, 6)
+    k_d4_pair2d(const float* __restrict__ U, float* __restrict__ Un, const float* __restrict__ F, float lam,
+                float tau, float isg2, Dims d, int zc, const StopCtl* ctl, double2* partials) {
+    __shared__ __align__(16) float sU[TP2];
+    __shared__ __align__(16) float sW[TP2];
+    const float EPS = 1.0e-7f;
+    const float2 HALF2 = splat(0.5f), QUART2 = splat(0.25f), TWO2 = splat(2.0f), MTWO2 = splat(-2.0f);
+    const float2 ONE2 = splat(1.0f), isg22 = splat(isg2), tau2 = splat(tau), mlam2 = splat(-lam);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int X = d4_tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first pixel
+    const int y = blockIdx.y * OY2 - 2 + ty;
+    const bool upd = tx >= 1 && tx <= PX - 2 && ty >= 2 && ty <= ROWS2 - 3 && X >= 0 && X < nx && y >= 0 && y < ny;
+    const int o = ty * TW + 2 * tx;
+    const int rowlo = ty * TW, rowhi = rowlo + TW - 1;
+    const int dxl = ((X == 0) ? o + 1 : max(o - 1, rowlo)) - o;
+    const int dxh = ((X + 2 == nx) ? o : min(o + 2, rowhi)) - o;
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    yl = min(max(yl, 0), ROWS2 - 1);
+    yh = min(max(yh, 0), ROWS2 - 1);
+    const int oyl = yl * TW + 2 * tx, oyh = yh * TW + 2 * tx;
+    const int col = min(max(y, 0), ny - 1) * nx + min(max(X, 0), nx - 2);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+    const float2 fv = ldg2(F + col);  // f never changes during a run: loaded before the wait
+    pdl_wait();                       // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    const float2 u = ldg2(U + col);
+    st2(sU + o, u);
+    __syncthreads();
+    {
+        const float2 lo = make_float2(sU[o + dxl], u.x), hi = make_float2(u.y, sU[o + dxh]);
+        const float2 ml = ld2(sU + oyl), mh = ld2(sU + oyh);
+        const float2 mll = make_float2(sU[oyl + dxl], ml.x), mlh = make_float2(ml.y, sU[oyl + dxh]);
+        const float2 mhl = make_float2(sU[oyh + dxl], mh.x), mhh = make_float2(mh.y, sU[oyh + dxh]);
+        const float2 gx = mul2(HALF2, sub2(lo, hi));
+        const float2 gy = mul2(HALF2, sub2(ml, mh));
+        const float2 gx2 = mul2(gx, gx), gy2 = mul2(gy, gy);
+        const float2 gxx = fma2(MTWO2, u, add2(lo, hi));
+        const float2 gyy = fma2(MTWO2, u, add2(ml, mh));
+        const float2 gxy = mul2(QUART2, sub2(sub2(add2(mll, mhh), mhl), mlh));
+        const float2 xy2 = mul2(mul2(mul2(TWO2, gx), gy), gxy);
+        const float2 den = add2(gx2, gy2);
+        const float2 nn = fma2(gyy, gy2, fma2(gxx, gx2, xy2));
+        const float2 oo = fma2(gyy, gx2, fma2(gxx, gy2, neg2(xy2)));
+        const float2 iq = rcp2(make_float2((den.x <= EPS) ? EPS : den.x, (den.y <= EPS) ? EPS : den.y));
+        const float2 vn = mul2(nn, iq), vo = mul2(oo, iq);
+        const float2 c = rcp2(fma2(den, isg22, ONE2));
+        st2(sW + o, fma2(mul2(c, c), vn, mul2(c, vo)));
+    }
+    __syncthreads();
+    float pa = 0.f, pb = 0.f;
+    if (upd) {
+        const float2 w = ld2(sW + o);
+        const float2 lx = fma2(MTWO2, w, add2(make_float2(sW[o + dxl], w.x), make_float2(w.y, sW[o + dxh])));
+        const float2 ly = fma2(MTWO2, w, add2(ld2(sW + oyl), ld2(sW + oyh)));
+        const float2 lap = add2(lx, ly);
+        const float2 un = fma2(tau2, fma2(mlam2, lap, neg2(sub2(u, fv))), u);
+        float* dst = Un + col;
+        if (ALIGNED) {
+            st2(dst, un);
+        } else {
+            dst[0] = un.x;
+            dst[1] = un.y;
+        }
+        if (CHECK) {
+            const float2 df = sub2(un, u);
+            pa = df.x * df.x + df.y * df.y;
+            pb = un.x * un.x + un.y * un.y;
+        }
+    }
+    if (CHECK) block_pair_partial<NTP2>(pa, pb, partials, block_slot());
+}
+
 // 32 rows: two CTAs (32 warps) per SM; 16 rows (four CTAs) measured the same
 // at 512^3 (0.824 ms per iteration) and 3% slower at 256^3
 constexpr int ROWS = 32;
@@ -225,17 +312,29 @@ PairKernel pick(bool check, bool aligned) {
     return check ? k_d4_pair<true, false, ROWS> : k_d4_pair<false, false, ROWS>;
 }
 
+PairKernel pick2d(bool check, bool aligned) {
+    if (aligned) return check ? k_d4_pair2d<true, true> : k_d4_pair2d<false, true>;
+    return check ? k_d4_pair2d<true, false> : k_d4_pair2d<false, false>;
+}
+
 }  // namespace
 
 bool d4_pair_applies(const Dims& d) {
     // CILREG_D4_KERNEL=stream (or simple) keeps a one-voxel kernel
     const char* e = getenv("CILREG_D4_KERNEL");
-    return d.nz > 1 && d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
+    return d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
 }
 
 D4Plan d4_pair_plan(const Dims& d) {
     D4Plan T;
     T.pair = true;
+    if (d.nz == 1) {
+        T.block = dim3(PX, ROWS2, 1);
+        T.zchunk = 1;
+        T.grid = dim3((d.nx + OX4 - 1) / OX4, (d.ny + OY2 - 1) / OY2, 1);
+        T.nblocks = (long long)T.grid.x * T.grid.y;
+        return T;
+    }
     T.block = dim3(PX, ROWS, 1);
     const int gx = (d.nx + OX4 - 1) / OX4, gy = (d.ny + Geo<ROWS>::OY - 1) / Geo<ROWS>::OY;
     int resident = 0;
@@ -252,8 +351,8 @@ D4Plan d4_pair_plan(const Dims& d) {
 int d4_pair_step(const D4Plan& T, const float* cur, float* nxt, const float* f, float lam, float tau, float isg2,
                  const Dims& d, const StopCtl* ctl, int check, double2* partials, cudaStream_t s) {
     const bool aligned = host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f);
-    CILREG_CUDA(launch_pdl(pick(check != 0, aligned), T.grid, T.block, 0, s, cur, nxt, f, lam, tau, isg2, d,
-                           T.zchunk, ctl, partials));
+    CILREG_CUDA(launch_pdl(d.nz == 1 ? pick2d(check != 0, aligned) : pick(check != 0, aligned), T.grid, T.block, 0,
+                           s, cur, nxt, f, lam, tau, isg2, d, T.zchunk, ctl, partials));
     return OK;
 }
 

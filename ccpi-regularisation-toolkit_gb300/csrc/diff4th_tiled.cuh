@@ -12,9 +12,9 @@ struct D4Plan {
     bool pair = false;  // the two-voxels-per-thread kernel (diff4th_pair.cu)
 };
 
-// the plan of the streaming kernel that runs for `d`: 3D volumes with nx even
-// and fewer than 2^31 voxels run k_d4_pair (CILREG_D4_KERNEL=stream selects
-// k_d4_stream), others k_d4_stream
+// the plan of the streaming kernel that runs for `d`: volumes with nx even
+// and fewer than 2^31 voxels run k_d4_pair (3D) or k_d4_pair2d
+// (CILREG_D4_KERNEL=stream selects k_d4_stream), others k_d4_stream
 D4Plan d4_stream_plan(const Dims& d);
 bool d4_pair_applies(const Dims& d);
 D4Plan d4_pair_plan(const Dims& d);

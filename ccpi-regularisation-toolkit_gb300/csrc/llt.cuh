@@ -12,8 +12,8 @@ struct LltPlan {
     bool pair = false;  // the two-voxels-per-thread kernel (llt_pair.cu)
 };
 
-// 3D volumes with nx even and fewer than 2^31 voxels run k_llt_pair
-// (CILREG_LLT_KERNEL=stream selects k_llt_stream)
+// volumes with nx even and fewer than 2^31 voxels run k_llt_pair (3D) or
+// k_llt_pair2d (CILREG_LLT_KERNEL=stream selects k_llt_stream)
 bool llt_pair_applies(const Dims& d);
 LltPlan llt_pair_plan(const Dims& d);
 cudaError_t llt_pair_launch(const LltPlan& T, const float* cur, float* nxt, const float* f, float lam_rof,

@@ -225,12 +225,111 @@ __global__ void __launch_bounds__(NTP, MINB)
     if (CHECK) block_pair_partial<NTP>(pa.x + pa.y, pb.x + pb.y, partials, block_slot());
 }
 
+// One 2D iteration (nz == 1), two pixels per thread: the pair of a 16 x 16
+// CTA is loaded once, the ROF and LLT terms are formed on the inner 30 x 14
+// pixels into shared memory, the update on the inner 28 x 12
+// (LLT_ROF_core.c:104-152, 200-266, 404-436 in 2D).  Two barriers, no plane
+// loop.
+constexpr int ROWS2 = 16;
+constexpr int NTP2 = PX * ROWS2, TP2 = TW * ROWS2, OY2 = ROWS2 - 4;
+
+template <bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP2, 6)
+    k_llt_pair2d(const float* __restrict__ U, float* __restrict__ Un, const float* __restrict__ F, float lam_rof,
+                 float lam_llt, float tau, Dims d, int zc, const StopCtl* ctl, double2* partials) {
+    __shared__ __align__(16) float sU[TP2];
+    __shared__ __align__(16) float sR1[TP2];  // ROF D1 (j axis), read at j-1
+    __shared__ __align__(16) float sR2[TP2];  // ROF D2 (i axis), read at i-1
+    __shared__ __align__(16) float sL1[TP2];  // LLT i term, read at i+-1
+    __shared__ __align__(16) float sL2[TP2];  // LLT j term, read at j+-1
+    const float2 EPS2 = splat(1.0e-12f), MTWO2 = splat(-2.0f);
+    const float2 tau2 = splat(tau), lrof2 = splat(lam_rof), mlllt2 = splat(-lam_llt);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int X = blockIdx.x * OX4 - 2 + 2 * tx;  // x of the pair's first pixel
+    const int y = blockIdx.y * OY2 - 2 + ty;
+    const bool upd = tx >= 1 && tx <= PX - 2 && ty >= 2 && ty <= ROWS2 - 3 && X >= 0 && X < nx && y >= 0 && y < ny;
+    const int o = ty * TW + 2 * tx;
+    const int rowlo = ty * TW, rowhi = rowlo + TW - 1;
+    const int dxl = ((X == 0) ? o + 1 : max(o - 1, rowlo)) - o;
+    const int dxh = ((X + 2 == nx) ? o : min(o + 2, rowhi)) - o;
+    int yl = (ny == 1) ? ty : ((y - 1 < 0) ? ty + 1 : ty - 1);
+    int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    yl = min(max(yl, 0), ROWS2 - 1);
+    yh = min(max(yh, 0), ROWS2 - 1);
+    const int oyl = yl * TW + 2 * tx, oyh = yh * TW + 2 * tx;
+    const int col = min(max(y, 0), ny - 1) * nx + min(max(X, 0), nx - 2);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+    auto lo_of = [&](const float* pl, float2 c) { return make_float2(pl[o + dxl], c.x); };
+    auto hi_of = [&](const float* pl, float2 c) { return make_float2(c.y, pl[o + dxh]); };
+    const float2 fv = ldg2(F + col);  // f never changes during a run: loaded before the wait
+    pdl_wait();                       // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    const float2 c = ldg2(U + col);
+    st2(sU + o, c);
+    __syncthreads();
+    {
+        const float2 cl = lo_of(sU, c), ch = hi_of(sU, c);
+        const float2 xp = sub2(ch, c), xm = sub2(c, cl);
+        const float2 uyh = ld2(sU + oyh), uyl = ld2(sU + oyl);
+        const float2 yp = sub2(uyh, c), ym = sub2(c, uyl);
+        const float2 mx2 = minmod_sq2(xp, xm), my2 = minmod_sq2(yp, ym);
+        st2(sR1 + o, normalise2(yp, add2(fma2(yp, yp, mx2), EPS2)));
+        st2(sR2 + o, normalise2(xp, add2(fma2(xp, xp, my2), EPS2)));
+        const float2 v1 = add2(fma2(MTWO2, c, ch), cl);
+        const float2 v2 = add2(fma2(MTWO2, c, uyh), uyl);
+        float2 t1 = llt_sign2(v1), t2 = llt_sign2(v2);
+        if (llt_divides2(v1) | llt_divides2(v2)) {
+            t1 = llt_quot2(v1);
+            t2 = llt_quot2(v2);
+        }
+        st2(sL1 + o, t1);
+        st2(sL2 + o, t2);
+    }
+    __syncthreads();
+    float pa = 0.f, pb = 0.f;
+    if (upd) {
+        const float2 w1 = ld2(sL1 + o), w2 = ld2(sL2 + o);
+        const float2 dxx = add2(fma2(MTWO2, w1, hi_of(sL1, w1)), lo_of(sL1, w1));
+        const float2 dyy = add2(fma2(MTWO2, w2, ld2(sL2 + oyh)), ld2(sL2 + oyl));
+        const float2 r1 = ld2(sR1 + o), r2 = ld2(sR2 + o);
+        const float2 dv1 = sub2(r1, ld2(sR1 + oyl));
+        const float2 dv2 = sub2(r2, lo_of(sR2, r2));
+        const float2 laplc = add2(dxx, dyy);
+        const float2 div = add2(dv1, dv2);
+        const float2 t = sub2(fma2(mlllt2, laplc, mul2(lrof2, div)), sub2(c, fv));
+        const float2 un = fma2(tau2, t, c);
+        float* dst = Un + col;
+        if (ALIGNED) {
+            st2(dst, un);
+        } else {
+            dst[0] = un.x;
+            dst[1] = un.y;
+        }
+        if (CHECK) {
+            const float2 df = sub2(un, c);
+            pa = df.x * df.x + df.y * df.y;
+            pb = un.x * un.x + un.y * un.y;
+        }
+    }
+    if (CHECK) block_pair_partial<NTP2>(pa, pb, partials, block_slot());
+}
+
 // four CTAs per SM at 64 registers (small spills): 0.879 ms per 512^3
 // iteration; a 16 x 32 CTA, two per SM, ran 0.882 ms, and three CTAs at 80
 // registers without spills 0.996 ms (against 0.933 ms, both before the sign
 // shortcut of llt_term1)
 constexpr int MINB = 4;
 using PairKernel = decltype(&k_llt_pair<false, true, MINB>);
+
+PairKernel pick2d(bool check, bool aligned) {
+    if (aligned) return check ? k_llt_pair2d<true, true> : k_llt_pair2d<false, true>;
+    return check ? k_llt_pair2d<true, false> : k_llt_pair2d<false, false>;
+}
 
 PairKernel pick(bool check, bool aligned) {
     if (aligned) return check ? k_llt_pair<true, true, MINB> : k_llt_pair<false, true, MINB>;
@@ -242,12 +341,19 @@ PairKernel pick(bool check, bool aligned) {
 bool llt_pair_applies(const Dims& d) {
     // CILREG_LLT_KERNEL=stream keeps the one-voxel kernel
     const char* e = getenv("CILREG_LLT_KERNEL");
-    return d.nz > 1 && d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
+    return d.nx % 2 == 0 && d.n < (1LL << 31) && !(e && e[0] != '\0' && e[0] != 'p');
 }
 
 LltPlan llt_pair_plan(const Dims& d) {
     LltPlan T;
     T.pair = true;
+    if (d.nz == 1) {
+        T.block = dim3(PX, ROWS2, 1);
+        T.zchunk = 1;
+        T.grid = dim3((d.nx + OX4 - 1) / OX4, (d.ny + OY2 - 1) / OY2, 1);
+        T.nblocks = (long long)T.grid.x * T.grid.y;
+        return T;
+    }
     T.block = dim3(PX, ROWS, 1);
     const int gx = (d.nx + OX4 - 1) / OX4, gy = (d.ny + OY4 - 1) / OY4;
     static const int resident = resident_ctas(pick(false, true), NTP);
@@ -261,8 +367,8 @@ cudaError_t llt_pair_launch(const LltPlan& T, const float* cur, float* nxt, cons
                             float lam_llt, float tau, const Dims& d, const StopCtl* ctl, int check,
                             double2* partials, cudaStream_t s) {
     const bool aligned = host_aligned8(cur) && host_aligned8(nxt) && host_aligned8(f);
-    return launch_pdl(pick(check != 0, aligned), T.grid, T.block, 0, s, cur, nxt, f, lam_rof, lam_llt, tau, d,
-                      T.zchunk, ctl, partials);
+    return launch_pdl(d.nz == 1 ? pick2d(check != 0, aligned) : pick(check != 0, aligned), T.grid, T.block, 0, s,
+                      cur, nxt, f, lam_rof, lam_llt, tau, d, T.zchunk, ctl, partials);
 }
 
 }  // namespace cilreg

@@ -55,6 +55,60 @@ def test_llt_rof_two_voxel_kernel_equals_one_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-4)
 
 
+PAIR_2D_SHAPES = [(130, 98), (1, 64), (7, 2), (2, 90), (65, 300), (29, 58)]
+PAIR_2D_CALLS = {
+    "LLT_ROF": (lambda R, x, e, info: R.LLT_ROF(x, 0.02, 0.01, 60, 0.001, e, device="gpu", infovector=info),
+                lambda x, e: O.llt_rof(x, 0.02, 0.01, 60, 0.001, e)),
+    "Diff4th": (lambda R, x, e, info: R.Diff4th(x, 0.8, 0.02, 60, 1e-4, e, device="gpu", infovector=info),
+                lambda x, e: O.diff4th(x, 0.8, 0.02, 60, 1e-4, e)),
+}
+
+
+@pytest.mark.parametrize("shape", PAIR_2D_SHAPES, ids=str)
+@pytest.mark.parametrize("reg", sorted(PAIR_2D_CALLS))
+def test_two_pixel_2d_kernels_match_oracle(reg, shape):
+    """2D images with an even row length run the two-pixel kernels
+    (k_llt_pair2d, k_d4_pair2d): several tiles in x and y, rows of two
+    pixels, a single row, against the oracle with the same stopping
+    iteration."""
+    from ccpi.filters import regularisers as R
+
+    call, oracle = PAIR_2D_CALLS[reg]
+    rng = np.random.default_rng(53 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for epsil in (0.0, 1e-3):
+        ref, iref = oracle(x, epsil)
+        info = np.zeros(2, np.float32)
+        got = call(R, x, epsil, info)
+        assert int(info[0]) == int(iref[0])
+        assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-4)
+
+
+@pytest.mark.parametrize("reg", sorted(PAIR_2D_CALLS))
+def test_two_pixel_2d_kernels_with_arrays_off_8_byte_alignment(reg):
+    """An input 4 bytes off an 8-byte boundary runs the 4-byte variant of the
+    2D two-pixel kernels, which gives the 8-byte variant's result bit for
+    bit."""
+    import torch
+    from ccpi.filters import regularisersCuPy as D
+
+    shape = (77, 130)
+    n = shape[0] * shape[1]
+    x = torch.from_numpy(np.random.default_rng(59).random(shape).astype(np.float32)).cuda()
+    outs = []
+    for off in (0, 1):
+        buf = torch.zeros(n + 2, device="cuda")
+        buf[off:off + n] = x.ravel()
+        t = buf[off:off + n].view(shape)
+        assert (t.data_ptr() % 8 == 0) == (off == 0)
+        if reg == "LLT_ROF":
+            outs.append(D.LLT_ROF(t, 0.02, 0.01, 40, 0.001))
+        else:
+            outs.append(D.Diff4th(t, 0.8, 0.02, 40, 1e-4))
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], outs[1])
+
+
 @pytest.mark.parametrize("shape", SHAPES, ids=str)
 def test_fgp_dtv_matches_oracle_on_odd_shapes(shape):
     from ccpi.filters.regularisers import FGP_dTV
