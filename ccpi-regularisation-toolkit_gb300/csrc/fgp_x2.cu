@@ -191,6 +191,103 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, con
     if (CHECK) block_pair_partial<NTP>(pa, pb, partials, block_slot());
 }
 
+// One 2D iteration (nz == 1) with the tile of x2_tile, without its plane
+// pipeline: R of the pair's pixels (FGP_TV_core.c:168-179), U = f - lambda
+// div R on the tile less its first row and column (:119-135), then P from
+// the forward differences of U and the projection (:137-166, utils.c:180-213)
+// on the inner 30 x 14 pixels; two barriers.
+template <bool CHECK, bool ALIGNED>
+__global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, const StopCtl* ctl,
+                                                      double2* partials) {
+    __shared__ __align__(16) float sR1[ROWS * TW];
+    __shared__ __align__(16) float sR2[ROWS * TW];
+    __shared__ __align__(16) float sU[ROWS * TW];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int X = tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first pixel
+    const int y = blockIdx.y * OYP - 1 + ty;
+    const bool in_xy = X >= 0 && X < nx && y >= 0 && y < ny;
+    const bool urow = in_xy && ty >= 1;
+    const bool ux = urow && tx >= 1;
+    const bool prow = urow && ty <= OYP;
+    const bool vx = prow && tx >= 1;
+    const bool vy = prow && tx <= PX - 2;
+    const bool xlast = (X + 2 == nx), ylast = (y == ny - 1);
+    const int o = ty * TW + 2 * tx;
+    const int oxl = max(o - 1, ty * TW);
+    const int oxh = min(o + 2, ty * TW + TW - 1);
+    const int oyl = max(ty - 1, 0) * TW + 2 * tx;
+    const int oyh = min(ty + 1, ROWS - 1) * TW + 2 * tx;
+    const int col = in_xy ? (y * nx + X) : 0;
+    const float2 lam2 = splat(a.lam), mp2 = splat(a.multip);
+    auto ldg2 = [&](const float* p) -> float2 {
+        if (ALIGNED) return __ldg(reinterpret_cast<const float2*>(p));
+        return make_float2(__ldg(p), __ldg(p + 1));
+    };
+    const float2 fv = in_xy ? ldg2(a.f + col) : splat(0.f);  // f never changes: loaded before the wait
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    float2 c1 = splat(0.f), o1 = splat(0.f), c2 = splat(0.f), o2 = splat(0.f);
+    if (in_xy) {
+        c1 = ldg2(a.pc[0] + col);
+        o1 = ldg2(a.po[0] + col);
+        c2 = ldg2(a.pc[1] + col);
+        o2 = ldg2(a.po[1] + col);
+    }
+    float2 uo = splat(0.f);
+    if (CHECK && prow) {
+        const float* q = a.u + col;
+        uo = ALIGNED ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
+    }
+    const float2 cm = splat(a.carr ? a.carr[*a.cbase + a.coff] : a.c);
+    const float2 r1 = fma2(cm, sub2(c1, o1), c1);
+    const float2 r2 = fma2(cm, sub2(c2, o2), c2);
+    st2(sR1 + o, r1);
+    st2(sR2 + o, r2);
+    __syncthreads();
+    float2 u = splat(0.f);
+    if (urow) {
+        const float2 r1l = make_float2(sR1[oxl], r1.x);
+        const float2 s = sub2(sub2(add2(r1, r2), r1l), ld2(sR2 + oyl));
+        u = fma2(neg2(lam2), s, fv);
+        if (a.nonneg) u = make_float2(u.x < 0.f ? 0.f : u.x, u.y < 0.f ? 0.f : u.y);
+        if (!ux) u.x = 0.f;
+    }
+    st2(sU + o, u);
+    __syncthreads();
+    float pa = 0.f, pb = 0.f;
+    if (vx || vy) {
+        if (CHECK) {
+            const float2 df = sub2(u, uo);
+            const float2 dm = make_float2(vx ? df.x : 0.f, vy ? df.y : 0.f);
+            const float2 um = make_float2(vx ? u.x : 0.f, vy ? u.y : 0.f);
+            pa = dm.x * dm.x + dm.y * dm.y;
+            pb = um.x * um.x + um.y * um.y;
+        }
+        if (a.write_u) store_pair<ALIGNED>(a.u + col, u, vx, vy);
+        if (a.write_p) {
+            const float2 g1 = make_float2(u.x - u.y, xlast ? 0.f : u.y - sU[oxh]);
+            const float2 g2 = ylast ? splat(0.f) : sub2(u, ld2(sU + oyh));
+            float2 p1 = fma2(mp2, g1, r1);
+            float2 p2 = fma2(mp2, g2, r2);
+            if (!a.aniso) {
+                const float2 den = fma2(p2, p2, mul2(p1, p1));
+                const float2 sq = make_float2((den.x > 1.f) ? rsqrtf(den.x) : 1.f,
+                                              (den.y > 1.f) ? rsqrtf(den.y) : 1.f);
+                p1 = mul2(p1, sq);
+                p2 = mul2(p2, sq);
+            } else {
+                p1 = make_float2(unit_clip(p1.x), unit_clip(p1.y));
+                p2 = make_float2(unit_clip(p2.x), unit_clip(p2.y));
+            }
+            store_pair<ALIGNED>(a.pn[0] + col, p1, vx, vy);
+            store_pair<ALIGNED>(a.pn[1] + col, p2, vx, vy);
+        }
+    }
+    if (CHECK) block_pair_partial<NTP>(pa, pb, partials, block_slot());
+}
+
 // one iteration `it` of every volume of a batch (8-byte aligned arrays): a
 // flat grid over all volumes' tiles, P^j in ring[j mod 3] as in
 // k_fgp_stream_batch
@@ -276,9 +373,18 @@ TiledPlan fgp_x2_plan(const Dims& d) {
     const char* e = getenv("CILREG_FGP_KERNEL");
     // from 2^21 voxels (128^3): below it the one-voxel kernel's wave is as
     // fast (96^3: 11.8 against 13.0 us per iteration)
-    if (!(d.nz > 1 && d.nx % 2 == 0 && d.n >= (1LL << 21) && d.n < (1LL << 31) &&
-          !(e && e[0] != '\0' && e[0] != 'x')))
+    if (e && e[0] != '\0' && e[0] != 'x') return T;
+    if (d.nz == 1 && d.nx % 2 == 0 && d.n < (1LL << 31)) {
+        // 2D: every size (k_fgp_x2_2d)
+        T.use = true;
+        T.x2 = true;
+        T.block = dim3(PX, ROWS, 1);
+        T.zchunk = 1;
+        T.grid = dim3(tiles_x(d.nx), (d.ny + OYP - 1) / OYP, 1);
+        T.nblocks = (long long)T.grid.x * T.grid.y;
         return T;
+    }
+    if (!(d.nz > 1 && d.nx % 2 == 0 && d.n >= (1LL << 21) && d.n < (1LL << 31))) return T;
     T.use = true;
     T.x2 = true;
     T.block = dim3(PX, ROWS, 1);
@@ -314,6 +420,13 @@ int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const
     a.carr = carr;
     a.cbase = cbase;
     a.coff = coff;
+    if (d.nz == 1) {
+        X2Kernel k;
+        if (aligned) k = check ? k_fgp_x2_2d<true, true> : k_fgp_x2_2d<false, true>;
+        else k = check ? k_fgp_x2_2d<true, false> : k_fgp_x2_2d<false, false>;
+        CILREG_CUDA(launch_pdl(k, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
+        return OK;
+    }
     CILREG_CUDA(launch_pdl(pick(check != 0, aligned), T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
     return OK;
 }

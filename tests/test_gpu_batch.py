@@ -26,6 +26,9 @@ def test_fgp_batch_equals_single_calls(shapes, epsil, monkeypatch):
 
     vols = _volumes(shapes, 5)
     lams = [0.03 + 0.01 * i for i in range(len(vols))]
+    # a single 2D call with an even row length runs the two-pixel kernel; the
+    # batch runs the one-voxel kernel's arithmetic
+    monkeypatch.setenv("CILREG_FGP_KERNEL", "stream")
     for graph in ("1", "0"):
         monkeypatch.setenv("CILREG_BATCH_GRAPH", graph)
         infos = np.zeros((len(vols), 2), np.float32)
@@ -113,6 +116,7 @@ def test_fgp_persistent_batch_equals_single_calls(shapes, epsil, mode, monkeypat
     vols = _volumes(shapes, 9)
     lams = [0.03 + 0.01 * i for i in range(len(vols))]
     monkeypatch.setenv("CILREG_BATCH_MODE", mode)
+    monkeypatch.setenv("CILREG_FGP_KERNEL", "stream")  # the batch's one-voxel arithmetic in 2D too
     infos = np.zeros((len(vols), 2), np.float32)
     outs = FGP_TV_batch(vols, lams, 60, epsil, 0, 1, infovectors=infos)
     for v, o, lam, inf in zip(vols, outs, lams, infos):
