@@ -21,11 +21,11 @@
 //     calls whose GPU work overlaps (two streams, or two host threads) race
 //     on it and must be serialised by the caller;
 //   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture;
+//     (cudaGetSymbolAddress, with that device current);
 //   * a call waits for its stream before it returns (it reads the stop
-//     control back); with epsil != 0 it also reads the stop flag every
-//     twentieth iteration and stops enqueueing once the rule has fired.
+//     control back), so it cannot be captured into a CUDA graph; with
+//     epsil != 0 it also reads the stop flag every twentieth iteration and
+//     stops enqueueing once the rule has fired.
 #include <mutex>
 
 #include "../../include/cilreg_gb300.h"

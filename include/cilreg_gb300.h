@@ -269,10 +269,10 @@ int cilreg_debug_fail_allocations(int n);
  * Limits: at most 2^24 voxels (e.g. 256^3 or 4096^2), otherwise -2; with
  * epsil != 0 at most 2^18 reduction blocks.  All calls share the array:
  * calls whose GPU work overlaps race and must be serialised by the caller.
- * The first call on a device looks up the array's address on that device;
- * make it before any stream capture.  A call waits for its stream before it
- * returns; with epsil != 0 it reads the stop flag every twentieth iteration
- * and stops enqueueing once the rule has fired. */
+ * The first call on a device looks up the array's address on that device.
+ * A call waits for its stream before it returns, so it cannot be captured
+ * into a CUDA graph; with epsil != 0 it reads the stop flag every twentieth
+ * iteration and stops enqueueing once the rule has fired. */
 int cilreg_rof_tv_dev_noalloc(const float *d_in, float *d_out, float *infovector, const float *d_lambda,
                               float lambdaPar, int iters, float tau, float epsil, int dimX, int dimY, int dimZ,
                               void *stream);
