@@ -11,6 +11,8 @@
 // t_{k+1} is formed with a double square root as the reference does.
 #include <math.h>
 
+#include <vector>
+
 #include "drivers.cuh"
 #include "fgp_tiled.cuh"
 #include "nvtx.cuh"
@@ -59,7 +61,13 @@ int dtv_run(const float* f, const float* ref, float* u_out, float lam, int iters
     const bool three = d.nz > 1;
     const int nc = three ? 3 : 2;
     Scratch scratch(s);
-    TiledPlan T = fgp_tiled_plan(d);  // the streaming kernel is used whatever CILREG_FGP_KERNEL says
+    // 2D images with an even row length: the two-pixel kernel; otherwise the
+    // streaming kernel (whatever CILREG_FGP_KERNEL says, bar 'stream')
+    TiledPlan T = fgp_tiled_plan(d);
+    if (d.nz == 1) {
+        const TiledPlan X = fgp_x2_plan(d);
+        if (X.use) T = X;
+    }
     IterControl ctl(s, scratch, iters, epsil, T.nblocks);
     CILREG_TRY(ctl.status());
     float* ring[3][3] = {};
@@ -87,7 +95,45 @@ int dtv_run(const float* f, const float* ref, float* u_out, float lam, int iters
     }
     const float multip = three ? (1.0f / (26.0f * lam)) : (1.0f / (8.0f * lam));  // FGP_dTV_core.c:240, 338
     float tk = 1.0f, cprev = 0.0f;
-    for (int it = 0; it < iters; it++) {
+    // t_{k+1} = (1 + sqrt(1 + 4 t_k^2)) / 2 in double, as FGP_dTV_core.c:144
+    auto advance = [&]() {
+        const float tkp1 = (float)((1.0f + sqrt((double)(1.0f + 4.0f * tk * tk))) * 0.5f);
+        cprev = (tk - 1.0f) / tkp1;
+        tk = tkp1;
+    };
+    int it = 0;
+    constexpr int G = 66;  // replayed block: a multiple of the ring's period 3
+    if (!ctl.checking() && d.n <= (1LL << 22) && iters > 2 * G) {
+        // small image or volume, fixed count: iterations 0 .. iters-2 from a
+        // replayed graph, their momentum coefficients read on the device from
+        // the sequence formed here; the last one (U written, no P) directly
+        std::vector<float> cseq(iters);
+        for (int k = 0; k < iters; k++) {
+            cseq[k] = cprev;
+            advance();
+        }
+        float* carr = scratch.floats(iters);
+        int* cbase = (int*)scratch.bytes(sizeof(int));
+        if (!carr || !cbase) return scratch.status();
+        CILREG_CUDA(cudaMemcpyAsync(carr, cseq.data(), sizeof(float) * iters, cudaMemcpyHostToDevice, s));
+        CILREG_CUDA(cudaMemsetAsync(cbase, 0, sizeof(int), s));
+        auto iteration = [&](int k, cudaStream_t st, bool in_graph) -> int {
+            float* pn[3] = {ring[k % 3][0], ring[k % 3][1], ring[k % 3][2]};
+            const float* pc[3] = {ring[(k + 2) % 3][0], ring[(k + 2) % 3][1], ring[(k + 2) % 3][2]};
+            const float* po[3] = {ring[(k + 1) % 3][0], ring[(k + 1) % 3][1], ring[(k + 1) % 3][2]};
+            const int last = (k == iters - 1) ? 1 : 0;
+            CILREG_TRY(fgp_tiled_step(T, pc, po, pn, f, u_out, lam, cseq[k], multip, nonneg == 1, methodTV != 0, last,
+                                      1 - last, 0, d, ctl.ctl(), ctl.partials(), st, b, in_graph ? carr : nullptr,
+                                      cbase, k));
+            note_launch();
+            return OK;
+        };
+        CILREG_TRY(run_replayed(iters - 1, G, s, iteration,
+                                [&](cudaStream_t st) -> int { return fgp_advance_base(cbase, G, st); }));
+        CILREG_TRY(iteration(iters - 1, s, false));
+        it = iters;
+    }
+    for (; it < iters; it++) {
         const int check = ctl.is_check(it) ? 1 : 0;
         float* pn[3];
         const float* pc[3];
@@ -102,10 +148,7 @@ int dtv_run(const float* f, const float* ref, float* u_out, float lam, int iters
         CILREG_TRY(fgp_tiled_step(T, pc, po, pn, f, u_out, lam, cprev, multip, nonneg == 1, methodTV != 0, write_u,
                                   write_p, check, d, ctl.ctl(), ctl.partials(), s, b));
         note_launch();
-        // t_{k+1} = (1 + sqrt(1 + 4 t_k^2)) / 2 in double, as FGP_dTV_core.c:144
-        const float tkp1 = (float)((1.0f + sqrt((double)(1.0f + 4.0f * tk * tk))) * 0.5f);
-        cprev = (tk - 1.0f) / tkp1;
-        tk = tkp1;
+        advance();
         if (check) {
             CILREG_TRY(ctl.after_check(it, T.nblocks));
             if (ctl.host_should_stop()) break;

@@ -487,9 +487,9 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
                    const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                    int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
                    const float* const* b, const float* carr, const int* cbase, int coff) {
-    if (T.x2 && !b)
+    if (T.x2 && (!b || d.nz == 1))
         return fgp_x2_step(T, pc, po, pn, f, u, lam, c, multip, nonneg, aniso, write_u, write_p, check, d, ctl,
-                           partials, s, carr, cbase, coff);
+                           partials, s, carr, cbase, coff, b);
     TiledArgs a;
     a.carr = carr;
     a.cbase = cbase;

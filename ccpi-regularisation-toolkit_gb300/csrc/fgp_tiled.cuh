@@ -29,15 +29,16 @@ int fgp_tiled_step(const TiledPlan& T, const float* const pc[3], const float* co
 // *base += by on the device (one thread)
 int fgp_advance_base(int* base, int by, cudaStream_t s);
 
-// The iteration with two voxels per thread (fgp_x2.cu): 3D volumes with nx
-// even and fewer than 2^31 voxels (CILREG_FGP_KERNEL=stream or simple keep a
-// one-voxel kernel; use is false otherwise).  fgp_tiled_step runs it for a
-// plan with x2 set (not for FGP-dTV).
+// The iteration with two voxels per thread (fgp_x2.cu): 2D images and 3D
+// volumes of 2^21 voxels or more, nx even and fewer than 2^31 voxels
+// (CILREG_FGP_KERNEL=stream or simple keep a one-voxel kernel; use is false
+// otherwise).  fgp_tiled_step runs it for a plan with x2 set (FGP-dTV: 2D
+// images only, with `b` its reference's unit gradient).
 TiledPlan fgp_x2_plan(const Dims& d);
 int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                 const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                 int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
-                const float* carr, const int* cbase, int coff);
+                const float* carr, const int* cbase, int coff, const float* const* b = nullptr);
 
 // Two iterations k, k+1 in one streaming pass (fgp_pair.cu; 3D only).
 struct PairPlan {

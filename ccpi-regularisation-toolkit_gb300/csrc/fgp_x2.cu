@@ -48,6 +48,7 @@ struct X2Args {
     const float* carr;  // momentum from device memory (graph replays): carr[*cbase + coff]
     const int* cbase;
     int coff;
+    const float* b[2];  // FGP-dTV (2D kernel): unit gradient of the reference image
 };
 
 // One tile (bx, by, bz) of one volume: the whole CTA walks its z chunk and
@@ -195,8 +196,10 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, con
 // pipeline: R of the pair's pixels (FGP_TV_core.c:168-179), U = f - lambda
 // div R on the tile less its first row and column (:119-135), then P from
 // the forward differences of U and the projection (:137-166, utils.c:180-213)
-// on the inner 30 x 14 pixels; two barriers.
-template <bool CHECK, bool ALIGNED>
+// on the inner 30 x 14 pixels; two barriers.  DTV: the FGP-dTV iteration,
+// R and the gradient of U each taken onto the complement of the reference's
+// unit gradient b at the pixel (FGP_dTV_core.c:311-314, 350-356).
+template <bool CHECK, bool ALIGNED, bool DTV = false>
 __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, const StopCtl* ctl,
                                                       double2* partials) {
     __shared__ __align__(16) float sR1[ROWS * TW];
@@ -225,6 +228,11 @@ __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, 
         return make_float2(__ldg(p), __ldg(p + 1));
     };
     const float2 fv = in_xy ? ldg2(a.f + col) : splat(0.f);  // f never changes: loaded before the wait
+    float2 b1 = splat(0.f), b2 = splat(0.f);                  // neither does b
+    if (DTV && in_xy) {
+        b1 = ldg2(a.b[0] + col);
+        b2 = ldg2(a.b[1] + col);
+    }
     pdl_wait();  // the previous iteration has completed (launch_pdl)
     pdl_trigger();
     if (ctl->stop) return;
@@ -241,8 +249,13 @@ __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, 
         uo = ALIGNED ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
     }
     const float2 cm = splat(a.carr ? a.carr[*a.cbase + a.coff] : a.c);
-    const float2 r1 = fma2(cm, sub2(c1, o1), c1);
-    const float2 r2 = fma2(cm, sub2(c2, o2), c2);
+    float2 r1 = fma2(cm, sub2(c1, o1), c1);
+    float2 r2 = fma2(cm, sub2(c2, o2), c2);
+    if (DTV) {
+        const float2 ip = fma2(r2, b2, mul2(r1, b1));
+        r1 = fma2(neg2(ip), b1, r1);
+        r2 = fma2(neg2(ip), b2, r2);
+    }
     st2(sR1 + o, r1);
     st2(sR2 + o, r2);
     __syncthreads();
@@ -267,8 +280,13 @@ __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, 
         }
         if (a.write_u) store_pair<ALIGNED>(a.u + col, u, vx, vy);
         if (a.write_p) {
-            const float2 g1 = make_float2(u.x - u.y, xlast ? 0.f : u.y - sU[oxh]);
-            const float2 g2 = ylast ? splat(0.f) : sub2(u, ld2(sU + oyh));
+            float2 g1 = make_float2(u.x - u.y, xlast ? 0.f : u.y - sU[oxh]);
+            float2 g2 = ylast ? splat(0.f) : sub2(u, ld2(sU + oyh));
+            if (DTV) {
+                const float2 ip = fma2(g2, b2, mul2(g1, b1));
+                g1 = fma2(neg2(ip), b1, g1);
+                g2 = fma2(neg2(ip), b2, g2);
+            }
             float2 p1 = fma2(mp2, g1, r1);
             float2 p2 = fma2(mp2, g2, r2);
             if (!a.aniso) {
@@ -324,6 +342,7 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2_batch(const FgpBatchVol* __re
         a.carr = nullptr;
         a.cbase = nullptr;
         a.coff = 0;
+        a.b[0] = a.b[1] = nullptr;
         d = V.d;
     }
     __syncthreads();
@@ -399,9 +418,13 @@ TiledPlan fgp_x2_plan(const Dims& d) {
 int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const po[3], float* const pn[3],
                 const float* f, float* u, float lam, float c, float multip, int nonneg, int aniso, int write_u,
                 int write_p, int check, const Dims& d, const StopCtl* ctl, double2* partials, cudaStream_t s,
-                const float* carr, const int* cbase, int coff) {
+                const float* carr, const int* cbase, int coff, const float* const* b) {
+    if (b && d.nz != 1) return fail(ERR_ARG, __FILE__, __LINE__, "the two-voxel FGP-dTV iteration is 2D only");
     X2Args a;
     bool aligned = host_aligned8(f) && host_aligned8(u);
+    a.b[0] = b ? b[0] : nullptr;
+    a.b[1] = b ? b[1] : nullptr;
+    if (b) aligned = aligned && host_aligned8(b[0]) && host_aligned8(b[1]);
     for (int i = 0; i < 3; i++) {
         a.pc[i] = pc[i];
         a.po[i] = po[i];
@@ -422,8 +445,14 @@ int fgp_x2_step(const TiledPlan& T, const float* const pc[3], const float* const
     a.coff = coff;
     if (d.nz == 1) {
         X2Kernel k;
-        if (aligned) k = check ? k_fgp_x2_2d<true, true> : k_fgp_x2_2d<false, true>;
-        else k = check ? k_fgp_x2_2d<true, false> : k_fgp_x2_2d<false, false>;
+        if (b) {
+            if (aligned) k = check ? k_fgp_x2_2d<true, true, true> : k_fgp_x2_2d<false, true, true>;
+            else k = check ? k_fgp_x2_2d<true, false, true> : k_fgp_x2_2d<false, false, true>;
+        } else if (aligned) {
+            k = check ? k_fgp_x2_2d<true, true> : k_fgp_x2_2d<false, true>;
+        } else {
+            k = check ? k_fgp_x2_2d<true, false> : k_fgp_x2_2d<false, false>;
+        }
         CILREG_CUDA(launch_pdl(k, T.grid, T.block, 0, s, a, d, T.zchunk, ctl, partials));
         return OK;
     }

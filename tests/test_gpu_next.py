@@ -65,6 +65,9 @@ PAIR_2D_CALLS = {
                        lambda x, e: O.fgp_tv(x, 0.05, 60, e, 0, 1)),
     "FGP_aniso": (lambda R, x, e, info: R.FGP_TV(x, 0.05, 60, e, 1, 0, device="gpu", infovector=info),
                   lambda x, e: O.fgp_tv(x, 0.05, 60, e, 1, 0)),
+    "FGP_dTV": (lambda R, x, e, info: R.FGP_dTV(x, np.ascontiguousarray(x[::-1, ::-1]), 0.05, 60, e, 0.2, 0, 1,
+                                                device="gpu", infovector=info),
+                lambda x, e: O.dtv_fgp(x, np.ascontiguousarray(x[::-1, ::-1]), 0.05, 60, e, 0.2, 0, 1)),
 }
 
 
@@ -72,7 +75,7 @@ PAIR_2D_CALLS = {
 @pytest.mark.parametrize("reg", sorted(PAIR_2D_CALLS))
 def test_two_pixel_2d_kernels_match_oracle(reg, shape):
     """2D images with an even row length run the two-pixel kernels
-    (k_llt_pair2d, k_d4_pair2d, k_fgp_x2_2d): several tiles in x and y, rows of two
+    (k_llt_pair2d, k_d4_pair2d, k_fgp_x2_2d, also for FGP-dTV): several tiles in x and y, rows of two
     pixels, a single row, against the oracle with the same stopping
     iteration."""
     from ccpi.filters import regularisers as R
@@ -109,6 +112,8 @@ def test_two_pixel_2d_kernels_with_arrays_off_8_byte_alignment(reg):
             outs.append(D.LLT_ROF(t, 0.02, 0.01, 40, 0.001))
         elif reg == "Diff4th":
             outs.append(D.Diff4th(t, 0.8, 0.02, 40, 1e-4))
+        elif reg == "FGP_dTV":
+            outs.append(D.FGP_dTV(t, t.flip(0).contiguous(), 0.05, 40, 0.0, 0.2, 0, 1))
         else:
             outs.append(D.FGP_TV(t, 0.05, 40, 0.0, 1 if "aniso" in reg else 0, 1 if "nonneg" in reg else 0))
     torch.cuda.synchronize()

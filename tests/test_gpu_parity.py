@@ -251,6 +251,7 @@ REPLAY_CALLS = {
     "TGV": lambda R, x: R.TGV(x, 0.05, 1.0, 2.0, 300, 12.0, 0.0, device="gpu"),
     "NDF": lambda R, x: R.NDF(x, 0.02, 0.05, 300, 0.01, 1, 0.0, device="gpu"),
     "Diff4th": lambda R, x: R.Diff4th(x, 0.5, 0.05, 300, 0.0001, 0.0, device="gpu"),
+    "FGP_dTV": lambda R, x: R.FGP_dTV(x, np.ascontiguousarray(x[::-1]), 0.05, 300, 0.0, 0.2, 0, 1, device="gpu"),
 }
 
 
