@@ -55,7 +55,7 @@ def test_llt_rof_two_voxel_kernel_equals_one_voxel_kernel(shape, monkeypatch):
         assert np.max(np.abs(a - b)) <= rel_tol(b, 1e-4)
 
 
-PAIR_2D_SHAPES = [(130, 98), (1, 64), (7, 2), (2, 90), (65, 300), (29, 58)]
+PAIR_2D_SHAPES = [(130, 98), (1, 64), (7, 2), (2, 90), (65, 300), (29, 58), (257, 510)]
 PAIR_2D_CALLS = {
     "LLT_ROF": (lambda R, x, e, info: R.LLT_ROF(x, 0.02, 0.01, 60, 0.001, e, device="gpu", infovector=info),
                 lambda x, e: O.llt_rof(x, 0.02, 0.01, 60, 0.001, e)),

@@ -452,6 +452,22 @@ def test_ndf_streaming_kernel_equals_per_voxel_kernel(shape, penalty, monkeypatc
         monkeypatch.delenv("CILREG_NDF_KERNEL")
 
 
+@pytest.mark.parametrize("shape", [(64, 66), (33, 47), (10, 16, 22)], ids=str)
+@pytest.mark.parametrize("penalty", [1, 2, 3, 4, 5])
+def test_ndf_negative_sigma_matches_oracle(shape, penalty):
+    """A negative edge parameter: the kernels compare |e| with sigma/sqrt(2)
+    clamped at 0, which changes no comparison's outcome (only the sign of a
+    zero flux), and take the sign of e as a sign copy where |e| exceeds it;
+    the iterates match the oracle's (Jacobi sweeps)."""
+    from ccpi.filters.regularisers import NDF
+
+    rng = np.random.default_rng(61 + sum(shape) + penalty)
+    x = rng.random(shape).astype(np.float32)
+    ref, _ = O.ndf(x, 0.03, -0.08, 40, 0.01, penalty, 0.0, jacobi=True)
+    got = NDF(x, 0.03, -0.08, 40, 0.01, penalty, 0.0, device="gpu")
+    assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-5)
+
+
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (3, 29, 15), (67, 70, 9),
                                    (130, 33, 35)], ids=str)
 def test_sb_fused_sweeps_equal_per_sweep_kernels(shape, monkeypatch):
