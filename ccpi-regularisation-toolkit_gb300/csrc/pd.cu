@@ -5,6 +5,8 @@
 // kernel recomputes the projected dual at the voxel and at its three lower
 // neighbours, so P never makes a second pass through HBM.  Traffic per
 // voxel-iteration: read Ue, P(3), f; write Ue, P(3) -> 36 B in 3D.
+#include <string.h>
+
 #include "drivers.cuh"
 #include "pd_tiled.cuh"
 
@@ -112,7 +114,7 @@ int pd_run(const float* f, float* u_out, float lam, int iters, float epsil, floa
     const Launch3 L = plan_launch(d);
     // CILREG_PD_KERNEL=simple selects the per-voxel kernel (kept for A/B checks)
     const char* ek = getenv("CILREG_PD_KERNEL");
-    const bool stream = !(ek && ek[0] == 's');
+    const bool stream = !(ek && strcmp(ek, "simple") == 0);
     const PdPlan T = pd_stream_plan(d);
     const long long nparts = stream ? T.nblocks : num_blocks(L);
     IterControl ctl(s, scratch, iters, epsil, nparts);

@@ -15,6 +15,9 @@
 //   C. after one barrier, updates plane j-1: U = (clamp(Ue) - tau div P' +
 //      lt f) / (1 + lt), writes Ue' = U + theta (U - clamp(Ue)) and P'.
 // HBM traffic: read Ue, P(3), f; write Ue, P(3) -> 36 B per voxel (28 in 2D).
+#include <stdlib.h>
+#include <string.h>
+
 #include "pd_tiled.cuh"
 #include "pd_math.cuh"
 
@@ -133,6 +136,74 @@ __global__ void __launch_bounds__(NT, 3) k_pd_stream(PdStreamArgs a, Dims d, int
     if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
 }
 
+// One 2D iteration (nz == 1) on the tile of k_pd_stream without its plane
+// pipeline: Ue, the dual and f of the image are loaded at once (f before the
+// wait on the previous iteration), then the dual (one barrier) and the primal
+// update (a second barrier), with k_pd_stream's expressions, so the iterates
+// are the same bit for bit.
+template <bool CHECK>
+__global__ void __launch_bounds__(NT, 3) k_pd_2d(PdStreamArgs a, Dims d, int zc, const StopCtl* ctl,
+                                                 double2* partials) {
+    __shared__ float sUe[BY][BX];
+    __shared__ float sP1[BY][BX];
+    __shared__ float sP2[BY][BX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nx = d.nx, ny = d.ny;
+    const int x = blockIdx.x * OX + tx - 1;
+    const int y = blockIdx.y * OY + ty - 1;
+    const bool in_xy = (x >= 0) && (x < nx) && (y >= 0) && (y < ny);
+    const bool p_pt = in_xy && tx <= BX - 2 && ty <= BY - 2;
+    const bool o_pt = in_xy && tx >= 1 && ty >= 1 && tx <= OX && ty <= OY;
+    const int xh = (nx == 1) ? tx : ((x + 1 >= nx) ? tx - 1 : tx + 1);
+    const int yh = (ny == 1) ? ty : ((y + 1 >= ny) ? ty - 1 : ty + 1);
+    const int col = in_xy ? (y * nx + x) : 0;
+    const float fq = in_xy ? __ldg(a.f + col) : 0.f;  // f never changes: loaded before the wait
+    pdl_wait();  // the previous iteration has completed (launch_pdl)
+    pdl_trigger();
+    if (ctl->stop) return;
+    float c = 0.f, q1 = 0.f, q2 = 0.f;
+    if (in_xy) {
+        c = __ldg(a.u + col);
+        q1 = __ldg(a.p[0] + col);
+        q2 = __ldg(a.p[1] + col);
+    }
+    sUe[ty][tx] = c;
+    __syncthreads();
+    float p1 = 0.f, p2 = 0.f, p3 = 0.f;
+    if (p_pt) {
+        p1 = pd_dual(q1, a.sigma, sUe[ty][xh], c);
+        p2 = pd_dual(q2, a.sigma, sUe[yh][tx], c);
+        if (!a.aniso) {
+            pd_project_iso<false>(p1, p2, p3);
+        } else {
+            p1 = pd_project_aniso(p1);
+            p2 = pd_project_aniso(p2);
+        }
+        sP1[ty][tx] = p1;
+        sP2[ty][tx] = p2;
+    }
+    __syncthreads();
+    float pa = 0.f, pb = 0.f;
+    if (o_pt) {
+        const float d1 = (x == 0) ? -p1 : -(p1 - sP1[ty][tx - 1]);
+        const float d2 = (y == 0) ? -p2 : -(p2 - sP2[ty - 1][tx]);
+        const float dv = d1 + d2;
+        float uc = c;
+        if (a.nonneg && uc < 0.f) uc = 0.f;
+        const float unew = pd_primal(uc, a.tau, dv, a.lt, fq, a.onelt);
+        if (CHECK) {
+            const float df = unew - uc;
+            pa = df * df;
+            pb = unew * unew;
+            a.ubrk[col] = unew;
+        }
+        a.un[col] = pd_extrapolate(unew, a.theta, uc);
+        a.pn[0][col] = p1;
+        a.pn[1][col] = p2;
+    }
+    if (CHECK) block_pair_partial<NT>(pa, pb, partials, block_slot());
+}
+
 }  // namespace
 
 PdPlan pd_stream_plan(const Dims& d) {
@@ -154,7 +225,12 @@ int pd_stream_step(const PdPlan& T, const PdStreamArgs& a, const Dims& d, const 
                    cudaStream_t s) {
     const bool three = d.nz > 1, check = a.check != 0;
     decltype(&k_pd_stream<true, true, int>) kern;
-    if (d.n < (1LL << 31))
+    // 2D images below 2^31 pixels: the kernel without the plane pipeline
+    // (CILREG_PD_KERNEL=stream keeps the streaming kernel)
+    const char* ek = getenv("CILREG_PD_KERNEL");
+    if (!three && d.n < (1LL << 31) && !(ek && strcmp(ek, "stream") == 0))
+        kern = check ? k_pd_2d<true> : k_pd_2d<false>;
+    else if (d.n < (1LL << 31))
         kern = three ? (check ? k_pd_stream<true, true, int> : k_pd_stream<true, false, int>)
                      : (check ? k_pd_stream<false, true, int> : k_pd_stream<false, false, int>);
     else

@@ -526,6 +526,25 @@ def test_rof_per_voxel_lambda_matches_oracle(shape, monkeypatch):
         assert np.max(np.abs(got - ref)) <= rel_tol(ref, 1e-5)
 
 
+@pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (2, 2), (130, 97), (61, 300), (257, 31)], ids=str)
+def test_pd_2d_kernel_equals_streaming_kernel(shape, monkeypatch):
+    """2D images run a PD kernel without the plane pipeline (k_pd_2d); its
+    expressions are the streaming kernel's, so the iterates and the stopping
+    iterations are the same bit for bit."""
+    from ccpi.filters.regularisers import PD_TV
+
+    rng = np.random.default_rng(19 + sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    for method, nonneg, epsil in ((0, 1, 3e-4), (1, 0, 0.0), (0, 0, 0.0)):
+        ia, ib = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        a = PD_TV(x, 0.05, 70, epsil, 8.0, method, nonneg, device="gpu", infovector=ia)
+        monkeypatch.setenv("CILREG_PD_KERNEL", "stream")
+        b = PD_TV(x, 0.05, 70, epsil, 8.0, method, nonneg, device="gpu", infovector=ib)
+        monkeypatch.delenv("CILREG_PD_KERNEL")
+        assert int(ia[0]) == int(ib[0])
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("shape", [(40, 56), (1, 33), (33, 1), (10, 16, 22), (2, 30, 31), (67, 70, 9), (130, 33, 35)],
                          ids=str)
 def test_pd_streaming_kernel_equals_per_voxel_kernel(shape, monkeypatch):
