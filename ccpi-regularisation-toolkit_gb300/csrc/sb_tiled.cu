@@ -269,13 +269,15 @@ __global__ void __launch_bounds__(NT, 2) k_sb_fused(SbFusedArgs a, Dims d, int z
     float pa = 0.f, pb = 0.f;
 
     if constexpr (!THREE) {
-        // one plane: D, B from U and B_prev; both sweeps (SB_TV_core.c:166-248)
+        // one plane: D, B from U and B_prev; both sweeps (SB_TV_core.c:166-248);
+        // every load issued before the first barrier
         const float u0 = __ldg(a.u + col), fv = __ldg(a.f + col);
+        const float bp1 = __ldg(a.bp[0] + col), bp2 = __ldg(a.bp[1] + col);
         sU0[0][oc] = u0;
         __syncthreads();
         float dx, dy, dz, bx, by, bz;
-        sb_shrink<false, ANISO>(sU0[0][oxh] - u0, sU0[0][oyh] - u0, 0.f, __ldg(a.bp[0] + col),
-                                __ldg(a.bp[1] + col), 0.f, dlam, dx, dy, dz, bx, by, bz);
+        sb_shrink<false, ANISO>(sU0[0][oxh] - u0, sU0[0][oyh] - u0, 0.f, bp1, bp2, 0.f, dlam, dx, dy, dz, bx, by,
+                                bz);
         if (o_pt) {
             a.bn[0][col] = bx;
             a.bn[1][col] = by;

@@ -107,6 +107,10 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a1, Dims d1
     if constexpr (!THREE) {
         const float p1 = __ldg(tab[0] + col), p2 = __ldg(tab[1] + col);
         const float q1 = __ldg(tab[3 + 0] + col), q2 = __ldg(tab[3 + 1] + col), q3 = __ldg(tab[3 + 2] + col);
+        // the pixel's own U, U0 and V, issued with the rest before the barrier
+        // (each pixel is written only by its own thread)
+        const float uo = tab[12][col], u0 = __ldg(tab[13] + col);
+        const float v1 = tab[9 + 0][col], v2 = tab[9 + 1][col];
         sm[0][0][oc] = p1;
         sm[0][1][oc] = p2;
         sm[0][2][oc] = q1;
@@ -116,8 +120,7 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a1, Dims d1
         if (o_pt) {
             // DivProjP_2D + newU (TGV_core.c:277-298, 300-306)
             const float dv = bwd(p1, sm[0][0][ox], xf, xl) + bwd(p2, sm[0][1][oy], yf, yl);
-            const float uo = tab[12][col];
-            const float un = (lam * (uo + tau * dv) + tau * __ldg(tab[13] + col)) * ilt;
+            const float un = (lam * (uo + tau * dv) + tau * u0) * ilt;
             const float ue = 2.0f * un - uo;
             tab[12][col] = ue;
             if (CHECK) {
@@ -128,7 +131,6 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_primal_stream(TgvArgs a1, Dims d1
             // UpdV_2D + newV (TGV_core.c:308-345)
             const float d1 = bwd(q1, sm[0][2][ox], xf, xl) + bwd(q3, sm[0][4][oy], yf, yl);
             const float d2 = bwd(q3, sm[0][4][ox], xf, xl) + bwd(q2, sm[0][3][oy], yf, yl);
-            const float v1 = tab[9 + 0][col], v2 = tab[9 + 1][col];
             tab[9 + 0][col] = 2.0f * (v1 + tau * (p1 + d1)) - v1;
             tab[9 + 1][col] = 2.0f * (v2 + tau * (p2 + d2)) - v2;
         }
@@ -278,14 +280,18 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_dual_stream(TgvArgs a1, Dims d1, 
 
     if constexpr (!THREE) {
         const float u = __ldg(tab[12] + col), v1 = __ldg(tab[9] + col), v2 = __ldg(tab[10] + col);
+        // the pixel's own P and Q, issued before the barrier (each pixel is
+        // written only by its own thread)
+        const float pold1 = tab[0][col], pold2 = tab[1][col];
+        const float qold1 = tab[3][col], qold2 = tab[4][col], qold3 = tab[5][col];
         sm[0][0][oc] = u;
         sm[0][1][oc] = v1;
         sm[0][2][oc] = v2;
         __syncthreads();
         if (o_pt) {
             // DualP_2D + ProjP_2D (TGV_core.c:200-232)
-            float p1 = tab[0][col] + (xe ? sigma * (-v1) : sigma * ((sm[0][0][ox] - u) - v1));
-            float p2 = tab[1][col] + (ye ? sigma * (-v2) : sigma * ((sm[0][0][oy] - u) - v2));
+            float p1 = pold1 + (xe ? sigma * (-v1) : sigma * ((sm[0][0][ox] - u) - v1));
+            float p2 = pold2 + (ye ? sigma * (-v2) : sigma * ((sm[0][0][oy] - u) - v2));
             const float gp = sqrtf(p1 * p1 + p2 * p2) / alpha1;
             if (gp > 1.0f) {
                 const float ig = __frcp_rn(gp);
@@ -304,9 +310,9 @@ __global__ void __launch_bounds__(NT, 2) k_tgv_dual_stream(TgvArgs a1, Dims d1, 
                 q2 = sm[0][2][oy] - v2;
                 q22 = sm[0][1][oy] - v1;
             }
-            float Q1 = tab[3][col] + sigma * q1;
-            float Q2 = tab[4][col] + sigma * q2;
-            float Q3 = tab[5][col] + sigma * (0.5f * (q11 + q22));
+            float Q1 = qold1 + sigma * q1;
+            float Q2 = qold2 + sigma * q2;
+            float Q3 = qold3 + sigma * (0.5f * (q11 + q22));
             float g = sqrtf(Q1 * Q1 + Q2 * Q2 + 2.0f * Q3 * Q3);
             g = g / alpha0;
             if (g > 1.0f) {
