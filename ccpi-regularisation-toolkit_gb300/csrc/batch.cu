@@ -9,7 +9,9 @@
 //     once (CILREG_BATCH_GRAPH=0: plain launches);
 //   * graph of two-voxel launches (FGP, 3D volumes with even x extents and
 //     8-byte aligned arrays): the same with the tiles of k_fgp_x2_batch
-//     (fgp_x2.cu), two voxels per thread;
+//     (fgp_x2.cu), two voxels per thread; chosen when every volume's single
+//     call runs the two-voxel kernel, so that a batch equals its single calls
+//     bit for bit;
 //   * persistent (FGP): one launch runs every iteration of every volume; its
 //     CTAs take (iteration, tile) items from a device-side queue and wait
 //     only for their own volume's previous iteration (k_fgp_persistent,
@@ -424,40 +426,58 @@ int fgp_run_schedule(const FgpSchedule& S, const BatchLayout& L, const float* co
 int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* const* u, const float* lams, int iters,
                         int methodTV, int nonneg, cudaStream_t s, FgpSchedule& out) {
     out = FgpSchedule();
+    const int nvol = (int)L.dims.size();
+    // A batch gives its volumes' single-call results bit for bit: when every
+    // volume's single call runs the two-voxel kernel (fgp.cu: 3D, even rows,
+    // 2^21 voxels up to the tensor-copy kernel's sizes), the batch runs
+    // two-voxel tiles; otherwise the one-voxel schedules, whose arithmetic is
+    // that of the streaming and tensor-copy kernels.
+    bool all_x2 = L.three && fgp_x2_batch_usable(L.dims.data(), f, u, nvol);
+    for (int v = 0; v < nvol && all_x2; v++) all_x2 = !fgp_tma_usable(L.dims[v]) && fgp_x2_plan(L.dims[v]).use;
     if (const char* m = getenv("CILREG_BATCH_MODE")) {
         // "graph", "x2" (graph of two-voxel launches), "persistent" or
         // "persistent:<MB>" (volume groups of at most MB of state)
         if (m[0] == 'p') {
             out.mode = 1;
             if (const char* c = strchr(m, ':')) out.group_mb = atoi(c + 1) < 0 ? 0 : atoi(c + 1) % 1000;
-        } else if (m[0] == 'x' && fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size())) {
+        } else if (m[0] == 'x' && fgp_x2_batch_usable(L.dims.data(), f, u, nvol)) {
             out.mode = 2;
         }
         return OK;
     }
+    if (all_x2) out.mode = 2;
     if (!L.three || iters < 8 || !env_flag("CILREG_BATCH_AUTOTUNE", true)) return OK;
     const std::string key = tune_key("fgp-schedule", L);
     const int c = cached_choice(key);
     if (c != 0) {
         out = FgpSchedule::from(c);
-        // the cache key holds the extents only: this call's arrays may not suit two-voxel tiles
-        if (out.mode == 2 && !fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size())) out.mode = 0;
+        // the cache key holds the extents only: keep the family of kernels
+        // this call's volumes and arrays give
+        if (all_x2 && out.mode != 2) {
+            out.mode = 2;
+            out.group_mb = 0;
+        } else if (!all_x2 && out.mode == 2) {
+            out.mode = 0;
+        }
         return OK;
     }
     std::vector<FgpSchedule> cand;
-    const int modes = fgp_x2_batch_usable(L.dims.data(), f, u, (int)L.dims.size()) ? 3 : 2;
-    for (int mode = 0; mode < modes; mode++)
+    for (int mode : {0, 1, 2}) {
+        if ((mode == 2) != all_x2) continue;
         for (int zc : {64, 32, 16}) {
             FgpSchedule t;
             t.mode = mode;
             t.zc = zc;
             cand.push_back(t);
         }
-    FgpSchedule grouped;
-    grouped.mode = 1;
-    grouped.zc = 16;
-    grouped.group_mb = 96;
-    cand.push_back(grouped);
+    }
+    if (!all_x2) {
+        FgpSchedule grouped;
+        grouped.mode = 1;
+        grouped.zc = 16;
+        grouped.group_mb = 96;
+        cand.push_back(grouped);
+    }
     float best = 1e30f;
     cudaEvent_t e0, e1;
     CILREG_CUDA(cudaEventCreate(&e0));
