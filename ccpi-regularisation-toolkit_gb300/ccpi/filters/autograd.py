@@ -84,8 +84,11 @@ class FGPTVFunction(torch.autograd.Function):
         lams = lam_t.expand(len(vols)) if lam_t.numel() == 1 else lam_t
         if lams.numel() != len(vols):
             raise ValueError("lam must be a scalar or hold one value per volume")
-        if len(vols) > 1:
-            # all volumes in one batched run (one graph launch, bit-equal to single calls)
+        if len(vols) > 1 and vols[0].dim() == 3:
+            # all volumes in one batched run (one graph launch, bit-equal to
+            # single calls; 2D images run one call each: a single 2D call with
+            # an even row length runs the two-pixel kernel, the 2D batch the
+            # one-pixel arithmetic)
             from .batch import FGP_TV_batch
 
             outs = FGP_TV_batch(vols, lams.tolist(), iterations, 0.0, methodTV, nonneg, f.device.index or 0)
