@@ -1,5 +1,6 @@
-// Fourth-order diffusion, 3D iteration with two voxels per thread along x
-// (reference arithmetic Diffus4th_order_core.c:103-265).
+// Fourth-order diffusion iteration with two voxels per thread along x
+// (reference arithmetic Diffus4th_order_core.c:103-265): 3D volumes and
+// (k_d4_pair2d) 2D images.
 //
 // The scheme of k_d4_stream (U through a four-plane shared-memory ring, the
 // weighted Laplacian W formed once per voxel into a two-plane ring, the

@@ -1,5 +1,6 @@
-// FGP-TV 3D iteration with two voxels per thread along x (arithmetic
-// FGP_TV_core.c:220-269, projection utils.c:180-213).
+// FGP-TV iteration with two voxels per thread along x (arithmetic
+// FGP_TV_core.c:220-269, projection utils.c:180-213): 3D volumes, 2D images
+// (also FGP-dTV, k_fgp_x2_2d) and batches of 3D volumes (k_fgp_x2_batch).
 //
 // The scheme of k_fgp_stream (R and U formed once per voxel, P of plane k-1
 // from U's forward differences one plane behind, two barriers per plane, the
@@ -9,7 +10,7 @@
 // the outputs move in 8-byte accesses, offsets and loop control serve two
 // voxels, and the additions, multiplications and fused multiply-adds of both
 // voxels issue as paired FP32 instructions.  The projection's reciprocal
-// square roots and divisions stay per voxel.
+// square roots and anisotropic clips stay per voxel.
 //
 // It runs on volumes of 2^21 to 2^25 voxels, where k_fgp_stream is bound by
 // instruction issue and by the latency of its waves rather than by DRAM (the

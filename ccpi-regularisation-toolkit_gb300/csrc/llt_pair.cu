@@ -1,5 +1,5 @@
-// LLT-ROF, 3D iteration with two voxels per thread along x (reference
-// arithmetic LLT_ROF_core.c:54-436).
+// LLT-ROF iteration with two voxels per thread along x (reference
+// arithmetic LLT_ROF_core.c:54-436): 3D volumes and (k_llt_pair2d) 2D images.
 //
 // The scheme of k_llt_stream (U through a four-plane shared-memory ring; the
 // ROF fluxes and the LLT second-difference terms of plane j-1 formed once per
@@ -8,7 +8,7 @@
 // doubled along x, as k_rof_pair does for ROF-TV: 8-byte accesses of U, f,
 // the terms and the output, offsets and loop control shared by two voxels,
 // and paired FP32 additions, multiplications and fused multiply-adds.  The
-// reciprocal square roots, minmods and the LLT terms' divisions stay per
+// reciprocal square roots, minmods and the LLT terms' sign copies stay per
 // voxel.
 //
 // Ring planes beyond the volume are loaded from its mirrored planes, so the
