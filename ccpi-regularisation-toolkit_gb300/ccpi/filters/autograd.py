@@ -86,9 +86,8 @@ class FGPTVFunction(torch.autograd.Function):
             raise ValueError("lam must be a scalar or hold one value per volume")
         if len(vols) > 1 and vols[0].dim() == 3:
             # all volumes in one batched run (one graph launch, bit-equal to
-            # single calls; 2D images run one call each: a single 2D call with
-            # an even row length runs the two-pixel kernel, the 2D batch the
-            # one-pixel arithmetic)
+            # single calls, whose kernel family the batch follows); 2D images
+            # run one call each
             from .batch import FGP_TV_batch
 
             outs = FGP_TV_batch(vols, lams.tolist(), iterations, 0.0, methodTV, nonneg, f.device.index or 0)

@@ -7,7 +7,7 @@
 //     grid of every volume's tiles, a finalize CTA per volume on check
 //     iterations; the whole loop is captured into one CUDA graph and launched
 //     once (CILREG_BATCH_GRAPH=0: plain launches);
-//   * graph of two-voxel launches (FGP, 3D volumes with even x extents and
+//   * graph of two-voxel launches (FGP, volumes with even x extents and
 //     8-byte aligned arrays): the same with the tiles of k_fgp_x2_batch
 //     (fgp_x2.cu), two voxels per thread; chosen when every volume's single
 //     call runs the two-voxel kernel, so that a batch equals its single calls
@@ -408,7 +408,7 @@ int fgp_run_schedule(const FgpSchedule& S, const BatchLayout& L, const float* co
     FgpBatch B;
     const bool x2 = S.mode == 2;
     if (x2 && !fgp_x2_batch_usable(L.dims.data(), f, u, nvol))
-        return fail(ERR_ARG, __FILE__, __LINE__, "two-voxel batch: a volume is 2D, has an odd x extent or misaligned arrays");
+        return fail(ERR_ARG, __FILE__, __LINE__, "two-voxel batch: a volume has an odd x extent or misaligned arrays");
     CILREG_TRY(fgp_build(B, sc, L, f, u, lams, S.zc, s, x2));
     CILREG_TRY(fgp_reset(B, nvol, iters, s));
     if (S.mode == 1 && iters > 0)
@@ -432,7 +432,7 @@ int fgp_choose_schedule(const BatchLayout& L, const float* const* f, float* cons
     // 2^21 voxels up to the tensor-copy kernel's sizes), the batch runs
     // two-voxel tiles; otherwise the one-voxel schedules, whose arithmetic is
     // that of the streaming and tensor-copy kernels.
-    bool all_x2 = L.three && fgp_x2_batch_usable(L.dims.data(), f, u, nvol);
+    bool all_x2 = fgp_x2_batch_usable(L.dims.data(), f, u, nvol);
     for (int v = 0; v < nvol && all_x2; v++) all_x2 = !fgp_tma_usable(L.dims[v]) && fgp_x2_plan(L.dims[v]).use;
     if (const char* m = getenv("CILREG_BATCH_MODE")) {
         // "graph", "x2" (graph of two-voxel launches), "persistent" or

@@ -117,8 +117,9 @@ void fgp_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz);
 int fgp_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, bool three, bool wide, int it,
                    float c, int nonneg, int aniso, int write_u, int write_p, int check, cudaStream_t s);
 
-// the same with the two-voxel tile (fgp_x2.cu): every volume 3D with nx even,
-// below 2^31 voxels, f and u 8-byte aligned; its tile grid per volume
+// the same with the two-voxel tile (fgp_x2.cu; the 2D tile for volumes of one
+// plane): every volume with nx even, below 2^31 voxels, f and u 8-byte
+// aligned; its tile grid per volume
 bool fgp_x2_batch_usable(const Dims* dims, const float* const* f, float* const* u, int nvol);
 void fgp_x2_tile_grid(const Dims& d, int zc, int& gx, int& gy, int& gz);
 int fgp_x2_batch_step(const FgpBatchVol* d_vols, const int* d_tile_vol, long long ntiles, int it, float c,

@@ -200,16 +200,19 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2(X2Args a, Dims d, int zc, con
 // on the inner 30 x 14 pixels; two barriers.  DTV: the FGP-dTV iteration,
 // R and the gradient of U each taken onto the complement of the reference's
 // unit gradient b at the pixel (FGP_dTV_core.c:311-314, 350-356).
-template <bool CHECK, bool ALIGNED, bool DTV = false>
-__global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, const StopCtl* ctl,
-                                                      double2* partials) {
+// Tile (bx, by) of one image; `wait` runs once f (and b) are loaded and
+// returns false when the run has stopped (the tile then does nothing and
+// returns false).
+template <bool CHECK, bool ALIGNED, bool DTV, class Wait>
+__device__ __forceinline__ bool x2_tile_2d(const X2Args& a, const Dims& d, int bx, int by, Wait wait, float& pa_out,
+                                           float& pb_out) {
     __shared__ __align__(16) float sR1[ROWS * TW];
     __shared__ __align__(16) float sR2[ROWS * TW];
     __shared__ __align__(16) float sU[ROWS * TW];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = d.nx, ny = d.ny;
-    const int X = tile_x0(blockIdx.x) + 2 * tx;  // x of the pair's first pixel
-    const int y = blockIdx.y * OYP - 1 + ty;
+    const int X = tile_x0(bx) + 2 * tx;  // x of the pair's first pixel
+    const int y = by * OYP - 1 + ty;
     const bool in_xy = X >= 0 && X < nx && y >= 0 && y < ny;
     const bool urow = in_xy && ty >= 1;
     const bool ux = urow && tx >= 1;
@@ -234,9 +237,7 @@ __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, 
         b1 = ldg2(a.b[0] + col);
         b2 = ldg2(a.b[1] + col);
     }
-    pdl_wait();  // the previous iteration has completed (launch_pdl)
-    pdl_trigger();
-    if (ctl->stop) return;
+    if (!wait()) return false;
     float2 c1 = splat(0.f), o1 = splat(0.f), c2 = splat(0.f), o2 = splat(0.f);
     if (in_xy) {
         c1 = ldg2(a.pc[0] + col);
@@ -304,12 +305,29 @@ __global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, 
             store_pair<ALIGNED>(a.pn[1] + col, p2, vx, vy);
         }
     }
-    if (CHECK) block_pair_partial<NTP>(pa, pb, partials, block_slot());
+    pa_out = pa;
+    pb_out = pb;
+    return true;
+}
+
+template <bool CHECK, bool ALIGNED, bool DTV = false>
+__global__ void __launch_bounds__(NTP, 8) k_fgp_x2_2d(X2Args a, Dims d, int zc, const StopCtl* ctl,
+                                                      double2* partials) {
+    float pa = 0.f, pb = 0.f;
+    const bool ran = x2_tile_2d<CHECK, ALIGNED, DTV>(a, d, blockIdx.x, blockIdx.y,
+                                                    [&]() {
+                                                        pdl_wait();  // the previous iteration has completed
+                                                        pdl_trigger();
+                                                        return !ctl->stop;
+                                                    },
+                                                    pa, pb);
+    if (CHECK && ran) block_pair_partial<NTP>(pa, pb, partials, block_slot());
 }
 
 // one iteration `it` of every volume of a batch (8-byte aligned arrays): a
 // flat grid over all volumes' tiles, P^j in ring[j mod 3] as in
-// k_fgp_stream_batch
+// k_fgp_stream_batch; a volume of one plane runs the 2D tile, as its single
+// call does
 template <bool CHECK>
 __global__ void __launch_bounds__(NTP, 4) k_fgp_x2_batch(const FgpBatchVol* __restrict__ vols,
                                                          const int* __restrict__ tile_vol, int it, float c,
@@ -348,7 +366,10 @@ __global__ void __launch_bounds__(NTP, 4) k_fgp_x2_batch(const FgpBatchVol* __re
     }
     __syncthreads();
     float pa = 0.f, pb = 0.f;
-    x2_tile<CHECK, true>(a, d, V.zc, bx, by, bz, pa, pb);
+    if (d.nz == 1)
+        x2_tile_2d<CHECK, true, false>(a, d, bx, by, []() { return true; }, pa, pb);
+    else
+        x2_tile<CHECK, true>(a, d, V.zc, bx, by, bz, pa, pb);
     if (CHECK) block_pair_partial<NTP>(pa, pb, V.partials, lt);
 }
 
@@ -363,8 +384,7 @@ X2Kernel pick(bool check, bool aligned) {
 
 bool fgp_x2_batch_usable(const Dims* dims, const float* const* f, float* const* u, int nvol) {
     for (int v = 0; v < nvol; v++)
-        if (dims[v].nz < 2 || dims[v].nx % 2 != 0 || dims[v].n >= (1LL << 31) || !host_aligned8(f[v]) ||
-            !host_aligned8(u[v]))
+        if (dims[v].nx % 2 != 0 || dims[v].n >= (1LL << 31) || !host_aligned8(f[v]) || !host_aligned8(u[v]))
             return false;
     return nvol > 0;
 }

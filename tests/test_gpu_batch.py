@@ -182,6 +182,25 @@ def test_fgp_two_voxel_batch_equals_single_calls(monkeypatch):
         np.testing.assert_array_equal(o.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("epsil", [0.0, 3e-4])
+def test_fgp_2d_batch_with_even_rows_equals_single_calls(epsil):
+    """2D images whose rows all have an even length: single calls run the
+    two-pixel kernel, and so does the batch (its 2D tile), so the batch gives
+    the single-call results bit for bit, with the same stopping iterations."""
+    from ccpi.filters.batch import FGP_TV_batch
+    from ccpi.filters.regularisers import FGP_TV
+
+    vols = _volumes([(37, 52), (128, 10), (200, 200), (1, 78), (300, 2)], 12)
+    lams = [0.03 + 0.01 * i for i in range(len(vols))]
+    infos = np.zeros((len(vols), 2), np.float32)
+    outs = FGP_TV_batch(vols, lams, 60, epsil, 0, 1, infovectors=infos)
+    for v, o, lam, inf in zip(vols, outs, lams, infos):
+        ref_info = np.zeros(2, np.float32)
+        ref = FGP_TV(v, lam, 60, epsil, 0, 1, device="gpu", infovector=ref_info)
+        assert int(inf[0]) == int(ref_info[0])
+        np.testing.assert_array_equal(o, ref)
+
+
 def test_batch_rejects_mixed_dimensionality():
     from ccpi.filters.batch import FGP_TV_batch
 
